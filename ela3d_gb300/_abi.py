@@ -1,0 +1,195 @@
+"""ctypes binding of libela3d.so (include/ela3d.h).
+
+There is no fallback: if the CUDA library is missing or cannot be loaded,
+``load_library`` raises.  The library is built in-tree by
+``ela3d_gb300._build.build_library`` (``__graft_entry__.build()`` runs it).
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from .params import CParams, FP64, ShotParams
+
+_LIB = None
+LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_build", "libela3d.so")
+
+# (name, restype, argtypes) of every entry point declared in include/ela3d.h
+_c = ctypes
+_P = _c.c_void_p
+SIGNATURES = [
+    ("ela3d_version", _c.c_char_p, []),
+    ("ela3d_status_string", _c.c_char_p, [_c.c_int]),
+    ("ela3d_last_error", _c.c_char_p, []),
+    ("ela3d_params_default", _c.c_int, [_c.POINTER(CParams)]),
+    ("ela3d_plan_create", _c.c_int, [_c.POINTER(CParams), _P, _P, _P, _c.POINTER(_P)]),
+    ("ela3d_run", _c.c_int, [_P, _c.c_int32]),
+    ("ela3d_enqueue", _c.c_int, [_P, _c.c_int32]),
+    ("ela3d_sync", _c.c_int, [_P]),
+    ("ela3d_get_seismograms", _c.c_int, [_P, _P]),
+    ("ela3d_get_seismograms_f64", _c.c_int, [_P, _P]),
+    ("ela3d_get_field", _c.c_int, [_P, _c.c_int32, _P]),
+    ("ela3d_get_field_f64", _c.c_int, [_P, _c.c_int32, _P]),
+    ("ela3d_energy", _c.c_int, [_P, _c.POINTER(_c.c_double)]),
+    ("ela3d_plan_info_get", _c.c_int, [_P, _P]),
+    ("ela3d_set_kernel_timing", _c.c_int, [_P, _c.c_int32]),
+    ("ela3d_get_kernel_timing", _c.c_int, [_P, _c.POINTER(_c.c_double), _c.POINTER(_c.c_double),
+                                           _c.POINTER(_c.c_int64), _c.POINTER(_c.c_int64)]),
+    ("ela3d_plan_destroy", _c.c_int, [_P]),
+    ("ela3d_variant_count", _c.c_int32, []),
+    ("ela3d_variant_get", _c.c_int, [_c.c_int32, _P]),
+    ("ela3d_plan_create_tuned", _c.c_int, [_c.POINTER(CParams), _P, _P, _P, _P, _c.POINTER(_P)]),
+]
+
+
+class PlanInfo(ctypes.Structure):
+    _fields_ = [("nx", ctypes.c_int32), ("ny", ctypes.c_int32), ("nz", ctypes.c_int32),
+                ("pitch_x", ctypes.c_int32), ("step", ctypes.c_int32), ("nsamp", ctypes.c_int32),
+                ("nrec", ctypes.c_int32), ("precision", ctypes.c_int32), ("device_bytes", ctypes.c_int64),
+                ("slab_lo", ctypes.c_int32 * 3), ("slab_hi", ctypes.c_int32 * 3)]
+
+
+class VariantInfo(ctypes.Structure):
+    _fields_ = [("fp64", ctypes.c_int32), ("tile_x", ctypes.c_int32), ("tile_y", ctypes.c_int32),
+                ("stages", ctypes.c_int32), ("threads", ctypes.c_int32), ("stress_smem", ctypes.c_int32),
+                ("velocity_smem", ctypes.c_int32)]
+
+
+class Tuning(ctypes.Structure):
+    _fields_ = [("variant", ctypes.c_int32), ("schedule", ctypes.c_int32), ("chunk", ctypes.c_int32),
+                ("blocks_per_sm", ctypes.c_int32)]
+
+
+def variants() -> list[VariantInfo]:
+    lib = load_library()
+    out = []
+    for i in range(lib.ela3d_variant_count()):
+        v = VariantInfo()
+        _check(lib.ela3d_variant_get(i, ctypes.byref(v)), "ela3d_variant_get")
+        out.append(v)
+    return out
+
+
+class Ela3dError(RuntimeError):
+    def __init__(self, status: int, where: str):
+        lib = _LIB
+        msg = lib.ela3d_status_string(status).decode() if lib else str(status)
+        detail = lib.ela3d_last_error().decode() if lib else ""
+        super().__init__(f"{where}: {msg} ({detail})")
+        self.status = status
+
+
+def load_library(path: str | None = None) -> ctypes.CDLL:
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = path or os.environ.get("ELA3D_LIB", LIB_PATH)
+    if not os.path.exists(path):
+        raise RuntimeError(f"libela3d.so not built ({path}); run __graft_entry__.build()")
+    lib = ctypes.CDLL(path)
+    for name, res, args in SIGNATURES:
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _LIB = lib
+    return lib
+
+
+def _check(st: int, where: str) -> None:
+    if st != 0:
+        raise Ela3dError(st, where)
+
+
+def _ptr(a: np.ndarray) -> int:
+    return a.ctypes.data
+
+
+class Plan:
+    """One shot resident on the GPU (ela3d_plan_create / ela3d_run / ...)."""
+
+    def __init__(self, params: ShotParams, cp: np.ndarray, cs: np.ndarray, rho: np.ndarray,
+                 variant: int = -1, schedule: int = -1, chunk: int = 0, blocks_per_sm: int = -1):
+        lib = load_library()
+        self._lib = lib
+        self.params = params
+        n = params.cells
+        models = [np.ascontiguousarray(a, dtype=np.float32).reshape(-1) for a in (cp, cs, rho)]
+        if any(m.size != n for m in models):
+            raise ValueError("model arrays must hold nx*ny*nz float32 values")
+        c, rec = params.to_c()
+        h = ctypes.c_void_p()
+        t = Tuning(variant, schedule, chunk, blocks_per_sm)
+        _check(lib.ela3d_plan_create_tuned(ctypes.byref(c), _ptr(models[0]), _ptr(models[1]), _ptr(models[2]),
+                                           ctypes.byref(t), ctypes.byref(h)), "ela3d_plan_create")
+        self._h = h
+
+    @property
+    def handle(self) -> ctypes.c_void_p:
+        return self._h
+
+    def run(self, nsteps: int) -> None:
+        _check(self._lib.ela3d_run(self._h, nsteps), "ela3d_run")
+
+    def enqueue(self, nsteps: int) -> None:
+        _check(self._lib.ela3d_enqueue(self._h, nsteps), "ela3d_enqueue")
+
+    def sync(self) -> None:
+        _check(self._lib.ela3d_sync(self._h), "ela3d_sync")
+
+    def seismograms(self, fp64: bool = False) -> np.ndarray:
+        p = self.params
+        out = np.zeros((p.nrec, 3, p.nsamp), np.float64 if fp64 else np.float32)
+        if out.size:
+            fn = self._lib.ela3d_get_seismograms_f64 if fp64 else self._lib.ela3d_get_seismograms
+            _check(fn(self._h, _ptr(out)), "ela3d_get_seismograms")
+        return out
+
+    def field(self, comp: int, fp64: bool = False) -> np.ndarray:
+        p = self.params
+        out = np.empty((p.nz, p.ny, p.nx), np.float64 if fp64 else np.float32)
+        fn = self._lib.ela3d_get_field_f64 if fp64 else self._lib.ela3d_get_field
+        _check(fn(self._h, comp, _ptr(out)), "ela3d_get_field")
+        return out
+
+    def energy(self) -> float:
+        e = ctypes.c_double()
+        _check(self._lib.ela3d_energy(self._h, ctypes.byref(e)), "ela3d_energy")
+        return e.value
+
+    def info(self) -> PlanInfo:
+        i = PlanInfo()
+        _check(self._lib.ela3d_plan_info_get(self._h, ctypes.byref(i)), "ela3d_plan_info_get")
+        return i
+
+    def set_kernel_timing(self, on: bool) -> None:
+        _check(self._lib.ela3d_set_kernel_timing(self._h, 1 if on else 0), "ela3d_set_kernel_timing")
+
+    def kernel_timing(self) -> tuple[float, float, int, int]:
+        a, b = ctypes.c_double(), ctypes.c_double()
+        na, nb = ctypes.c_int64(), ctypes.c_int64()
+        _check(self._lib.ela3d_get_kernel_timing(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(na),
+                                                 ctypes.byref(nb)), "ela3d_get_kernel_timing")
+        return a.value, b.value, na.value, nb.value
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) is not None and self._h.value:
+            self._lib.ela3d_plan_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def is_fp64(p: ShotParams) -> bool:
+    return p.precision == FP64

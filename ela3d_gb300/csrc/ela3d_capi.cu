@@ -1,0 +1,216 @@
+// ela3d_capi.cu -- the extern "C" entry points of include/ela3d.h.
+#include <cmath>
+#include <new>
+
+#include "ela3d_engine.h"
+
+using namespace ela3d;
+
+struct ela3d_plan {
+  std::unique_ptr<EngineBase> eng;
+  int fp64 = 0;
+  ela3d_params p{};
+};
+
+extern "C" {
+
+const char *ela3d_version(void) { return "ela3d-gb300 0.1"; }
+
+const char *ela3d_last_error(void) { return last_error(); }
+
+const char *ela3d_status_string(ela3d_status s) {
+  switch (s) {
+    case ELA3D_OK: return "ok";
+    case ELA3D_ERR_INVALID_ARG: return "invalid argument";
+    case ELA3D_ERR_OOM: return "out of device memory";
+    case ELA3D_ERR_CUDA: return "CUDA error";
+    case ELA3D_ERR_UNSTABLE: return "simulation unstable";
+    case ELA3D_ERR_TIMEOUT: return "device wait timed out";
+    case ELA3D_ERR_NO_DEVICE: return "no CUDA device";
+    case ELA3D_ERR_BUSY: return "busy";
+    case ELA3D_ERR_CANCELLED: return "cancelled";
+    case ELA3D_ERR_NOT_FOUND: return "not found";
+    case ELA3D_ERR_NOT_READY: return "not ready";
+  }
+  return "unknown status";
+}
+
+ela3d_status ela3d_params_default(ela3d_params *p) {
+  if (!p) return ELA3D_ERR_INVALID_ARG;
+  *p = ela3d_params{};
+  p->nx = p->ny = p->nz = 500;            // NIMX/NIMY/NIMZ
+  p->nstep = 1000;                        // NSTEP
+  p->dx = p->dy = p->dz = 10.0;           // DELTAX
+  p->dt = 1e-3;                           // DELTATT
+  p->npml = 10;                           // NPOINTS_PML
+  p->pml_mode = ELA3D_PML_COMPAT;
+  p->npower = 2.0;
+  p->k_max = 1.0;
+  p->alpha_max = -1.0;                    // 2*PI*(f0/2)
+  p->rcoef = 1e-3;
+  p->vpml = 3000.0;
+  p->f0 = 35.0;
+  p->t0 = 1.2 / 35.0;
+  p->factor = 1e7;
+  p->stf = ELA3D_STF_GAUSS_DERIV;
+  p->src_kind = ELA3D_SRC_EXPLOSIVE;
+  p->src_i = 501 / 2 - 1;                 // ISOURCE = DIMX/2 (1-based)
+  p->src_j = 501 / 2 - 1;
+  p->src_k = 11 - 1;                      // KSOURCE = 11 (1-based)
+  p->sampgat = 2;
+  p->src_w[0] = 0.0;
+  p->src_w[1] = 0.0;
+  p->src_w[2] = 1.0;
+  p->angle_force = 0.0;
+  p->rec = nullptr;
+  p->nrec = 0;
+  p->precision = ELA3D_FP32;
+  p->it_output = 200;
+  p->energy_every = 0;
+  return ELA3D_OK;
+}
+
+int32_t ela3d_variant_count(void) {
+  int n = 0;
+  variants(&n);
+  return n;
+}
+
+ela3d_status ela3d_variant_get(int32_t index, ela3d_variant_info *out) {
+  int n = 0;
+  const Variant *v = variants(&n);
+  if (!out || index < 0 || index >= n) return ELA3D_ERR_INVALID_ARG;
+  out->fp64 = v[index].fp64;
+  out->tile_x = v[index].tx;
+  out->tile_y = v[index].ty;
+  out->stages = v[index].ns;
+  out->threads = v[index].threads;
+  out->stress_smem = v[index].stress_smem;
+  out->velocity_smem = v[index].vel_smem;
+  return ELA3D_OK;
+}
+
+static TuneChoice resolve_tuning(const ela3d_params &p, const ela3d_tuning *t) {
+  TuneChoice c = default_choice(p.precision == ELA3D_FP64, p.nx, p.ny, p.nz);
+  if (!t) return c;
+  if (t->variant >= 0) c.variant = t->variant;
+  if (t->schedule >= 0) c.kind = t->schedule;
+  if (t->chunk > 0) c.chunk = t->chunk;
+  if (t->blocks_per_sm >= 0) c.blocks_per_sm = t->blocks_per_sm;
+  return c;
+}
+
+ela3d_status ela3d_plan_create_tuned(const ela3d_params *p, const float *cp, const float *cs, const float *rho,
+                                     const ela3d_tuning *tune, ela3d_plan **out) {
+  if (!p || !out) return ELA3D_ERR_INVALID_ARG;
+  *out = nullptr;
+  ela3d_status st = validate_params(*p);
+  if (st != ELA3D_OK) return st;
+  if (!cp || !cs || !rho) {
+    set_last_error("model arrays missing");
+    return ELA3D_ERR_INVALID_ARG;
+  }
+  ela3d_plan *plan = new (std::nothrow) ela3d_plan();
+  if (!plan) return ELA3D_ERR_OOM;
+  plan->fp64 = p->precision == ELA3D_FP64;
+  plan->p = *p;
+  plan->eng = make_engine(plan->fp64, &st);
+  if (st == ELA3D_OK) st = plan->eng->add_shot(*p, cp, cs, rho, -1);
+  const TuneChoice c = resolve_tuning(*p, tune);
+  if (st == ELA3D_OK) st = plan->eng->finalize(&c);
+  if (st != ELA3D_OK) {
+    delete plan;
+    return st;
+  }
+  plan->p.rec = nullptr;  // the engine keeps its own copy
+  *out = plan;
+  return ELA3D_OK;
+}
+
+ela3d_status ela3d_plan_create(const ela3d_params *p, const float *cp, const float *cs, const float *rho,
+                               ela3d_plan **out) {
+  return ela3d_plan_create_tuned(p, cp, cs, rho, nullptr, out);
+}
+
+ela3d_status ela3d_enqueue(ela3d_plan *plan, int32_t nsteps) {
+  if (!plan) return ELA3D_ERR_INVALID_ARG;
+  return plan->eng->enqueue(nsteps);
+}
+
+ela3d_status ela3d_sync(ela3d_plan *plan) {
+  if (!plan) return ELA3D_ERR_INVALID_ARG;
+  return plan->eng->sync();
+}
+
+ela3d_status ela3d_run(ela3d_plan *plan, int32_t nsteps) {
+  if (!plan) return ELA3D_ERR_INVALID_ARG;
+  if (nsteps < 0) return ELA3D_ERR_INVALID_ARG;
+  const int every = plan->p.energy_every;
+  if (every <= 0) {
+    ela3d_status st = plan->eng->enqueue(nsteps);
+    if (st != ELA3D_OK) return st;
+    return plan->eng->sync();
+  }
+  int left = nsteps;
+  while (left > 0) {
+    const int done = plan->eng->steps_done();
+    const int chunk = std::min(left, every - done % every);
+    ela3d_status st = plan->eng->enqueue(chunk);
+    if (st == ELA3D_OK) st = plan->eng->sync();
+    if (st != ELA3D_OK) return st;
+    left -= chunk;
+    if (plan->eng->steps_done() % every == 0) {
+      st = engine_check_energy(plan->eng.get(), 0, plan->fp64);
+      if (st != ELA3D_OK) return st;
+    }
+  }
+  return ELA3D_OK;
+}
+
+ela3d_status ela3d_get_seismograms(ela3d_plan *plan, float *out) {
+  if (!plan || !out) return ELA3D_ERR_INVALID_ARG;
+  return plan->eng->seismograms(0, out, 0);
+}
+
+ela3d_status ela3d_get_seismograms_f64(ela3d_plan *plan, double *out) {
+  if (!plan || !out) return ELA3D_ERR_INVALID_ARG;
+  return plan->eng->seismograms(0, out, 1);
+}
+
+ela3d_status ela3d_get_field(ela3d_plan *plan, int32_t comp, float *out) {
+  if (!plan || !out) return ELA3D_ERR_INVALID_ARG;
+  return plan->eng->field(0, comp, out, 0);
+}
+
+ela3d_status ela3d_get_field_f64(ela3d_plan *plan, int32_t comp, double *out) {
+  if (!plan || !out) return ELA3D_ERR_INVALID_ARG;
+  return plan->eng->field(0, comp, out, 1);
+}
+
+ela3d_status ela3d_energy(ela3d_plan *plan, double *out) {
+  if (!plan || !out) return ELA3D_ERR_INVALID_ARG;
+  return plan->eng->energy(0, out);
+}
+
+ela3d_status ela3d_plan_info_get(ela3d_plan *plan, ela3d_plan_info *out) {
+  if (!plan || !out) return ELA3D_ERR_INVALID_ARG;
+  return plan->eng->info(0, out);
+}
+
+ela3d_status ela3d_set_kernel_timing(ela3d_plan *plan, int32_t enable) {
+  if (!plan) return ELA3D_ERR_INVALID_ARG;
+  return plan->eng->set_timing(enable != 0);
+}
+
+ela3d_status ela3d_get_kernel_timing(ela3d_plan *plan, double *stress_ms, double *velocity_ms,
+                                     int64_t *stress_launches, int64_t *velocity_launches) {
+  if (!plan) return ELA3D_ERR_INVALID_ARG;
+  return plan->eng->timing(stress_ms, velocity_ms, stress_launches, velocity_launches);
+}
+
+ela3d_status ela3d_plan_destroy(ela3d_plan *plan) {
+  delete plan;
+  return ELA3D_OK;
+}
+
+}  // extern "C"

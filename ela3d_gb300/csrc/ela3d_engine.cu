@@ -1,0 +1,729 @@
+// ela3d_engine.cu -- host engine: device layout, C-PML slab sizing, tensor
+// maps, work schedule and the time-step loop.
+#include "ela3d_engine.h"
+
+#include <cudaTypedefs.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <numeric>
+
+namespace ela3d {
+
+static thread_local std::string g_last_error;
+void set_last_error(const std::string &m) { g_last_error = m; }
+const char *last_error() { return g_last_error.c_str(); }
+
+ela3d_status status_from_cuda(cudaError_t e, const char *what) {
+  if (e == cudaSuccess) return ELA3D_OK;
+  set_last_error(std::string(what) + ": " + cudaGetErrorString(e));
+  if (e == cudaErrorMemoryAllocation) return ELA3D_ERR_OOM;
+  if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) return ELA3D_ERR_NO_DEVICE;
+  return ELA3D_ERR_CUDA;
+}
+
+#define CK(call)                                              \
+  do {                                                        \
+    cudaError_t e_ = (call);                                  \
+    if (e_ != cudaSuccess) return status_from_cuda(e_, #call); \
+  } while (0)
+
+#define BAD(msg)                  \
+  do {                            \
+    set_last_error(msg);          \
+    return ELA3D_ERR_INVALID_ARG; \
+  } while (0)
+
+ela3d_status validate_params(const ela3d_params &p) {
+  if (p.nx < 3 || p.ny < 3 || p.nz < 3) BAD("grid must be at least 3 cells on each axis");
+  if ((long long)p.nx * p.ny * p.nz > (1ll << 34)) BAD("grid too large");
+  if (!(p.dx > 0 && p.dy > 0 && p.dz > 0 && p.dt > 0)) BAD("spacing and time step must be positive");
+  if (p.nstep < 0 || p.sampgat < 1) BAD("nstep must be >= 0 and sampgat >= 1");
+  if (p.npml < 0) BAD("npml must be >= 0");
+  if (p.npml > 0 && !(p.rcoef > 0 && p.rcoef < 1)) BAD("rcoef must lie in (0, 1)");
+  if (p.precision != ELA3D_FP32 && p.precision != ELA3D_FP64) BAD("precision must be FP32 or FP64");
+  if (p.pml_mode != ELA3D_PML_COMPAT && p.pml_mode != ELA3D_PML_CLEAN) BAD("unknown pml_mode");
+  if (p.stf < 0 || p.stf > 2) BAD("unknown stf");
+  if (p.src_kind != ELA3D_SRC_FORCE && p.src_kind != ELA3D_SRC_EXPLOSIVE) BAD("unknown src_kind");
+  if (p.src_i < 0 || p.src_i >= p.nx || p.src_j < 0 || p.src_j >= p.ny || p.src_k < 0 || p.src_k >= p.nz)
+    BAD("source outside the grid");
+  if (p.nrec < 0 || (p.nrec > 0 && !p.rec)) BAD("receiver list missing");
+  for (int r = 0; r < p.nrec; ++r) {
+    const int32_t *q = p.rec + 3 * r;
+    if (q[0] < 0 || q[0] >= p.nx || q[1] < 0 || q[1] >= p.ny || q[2] < 0 || q[2] >= p.nz)
+      BAD("receiver " + std::to_string(r) + " outside the grid");
+  }
+  return ELA3D_OK;
+}
+
+void slab_extent(const double *a_full, const double *a_half, int n, int *lo, int *hi) {
+  int l = 0, h = n;
+  for (int i = 0; i < n; ++i) {
+    const bool act = a_full[i] != 0.0 || a_half[i] != 0.0;
+    if (!act) continue;
+    if (2 * i < n) l = std::max(l, i + 1);
+    else h = std::min(h, i);
+  }
+  bool clean = l <= h;
+  for (int i = l; clean && i < h; ++i)
+    if (a_full[i] != 0.0 || a_half[i] != 0.0) clean = false;
+  if (!clean || l >= h) { l = n; h = n; }
+  *lo = l;
+  *hi = h;
+}
+
+void build_schedule(const std::vector<ShotShape> &shots, int tx, int ty, int kind, int chunk, int max_blocks,
+                    std::vector<Item> *items, std::vector<int2> *ranges) {
+  items->clear();
+  ranges->clear();
+  struct Col { int shot, tile, nz; };
+  std::vector<Col> cols;
+  long long units = 0;
+  for (int s = 0; s < (int)shots.size(); ++s) {
+    const int ntiles = ((shots[s].nx + tx - 1) / tx) * ((shots[s].ny + ty - 1) / ty);
+    for (int t = 0; t < ntiles; ++t) cols.push_back({s, t, shots[s].nz});
+    units += (long long)ntiles * shots[s].nz;
+  }
+  if (units == 0 || max_blocks < 1) return;
+  if (kind == 0) {
+    const long long G = std::min<long long>(max_blocks, units);
+    size_t ci = 0;
+    int kk = 0;  // next plane of cols[ci]
+    for (long long b = 0; b < G; ++b) {
+      long long take = (b + 1) * units / G - b * units / G;
+      const int first = (int)items->size();
+      while (take > 0) {
+        const Col &c = cols[ci];
+        const int run = (int)std::min<long long>(take, c.nz - kk);
+        items->push_back({c.shot, c.tile, kk, kk + run});
+        take -= run;
+        kk += run;
+        if (kk == c.nz) { ++ci; kk = 0; }
+      }
+      ranges->push_back(make_int2(first, (int)items->size()));
+    }
+    return;
+  }
+  // kind 1: z-chunks dealt round-robin in (shot, chunk, tile) order
+  if (chunk < 1) chunk = 1;
+  std::vector<Item> all;
+  for (int s = 0; s < (int)shots.size(); ++s) {
+    const int ntiles = ((shots[s].nx + tx - 1) / tx) * ((shots[s].ny + ty - 1) / ty);
+    for (int k0 = 0; k0 < shots[s].nz; k0 += chunk)
+      for (int t = 0; t < ntiles; ++t) all.push_back({s, t, k0, std::min(k0 + chunk, shots[s].nz)});
+  }
+  const int G = (int)std::min<long long>(max_blocks, (long long)all.size());
+  for (int b = 0; b < G; ++b) {
+    const int first = (int)items->size();
+    for (size_t q = b; q < all.size(); q += G) items->push_back(all[q]);
+    ranges->push_back(make_int2(first, (int)items->size()));
+  }
+}
+
+TuneChoice default_choice(int fp64, int nx, int ny, int nz) {
+  (void)nx; (void)ny; (void)nz;
+  int n = 0;
+  const Variant *v = variants(&n);
+  for (int i = 0; i < n; ++i) {
+    if (fp64 && v[i].fp64) return {i, 0, 16, 0};
+    if (!fp64 && !v[i].fp64) return {i, 0, 16, 0};
+  }
+  return {0, 0, 16, 0};
+}
+
+// ------------------------------------------------------------ TMA maps --
+static PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  });
+  return fn;
+}
+
+template <typename T>
+static ela3d_status encode_map(CUtensorMap *m, const T *base, int nx, int ny, int nz, int px, int bw, int bh) {
+  auto fn = encode_fn();
+  if (!fn) {
+    set_last_error("cuTensorMapEncodeTiled unavailable");
+    return ELA3D_ERR_CUDA;
+  }
+  cuuint64_t gdim[3] = {(cuuint64_t)nx, (cuuint64_t)ny, (cuuint64_t)nz};
+  cuuint64_t gstr[2] = {(cuuint64_t)px * sizeof(T), (cuuint64_t)px * ny * sizeof(T)};
+  cuuint32_t box[3] = {(cuuint32_t)bw, (cuuint32_t)bh, 1};
+  cuuint32_t es[3] = {1, 1, 1};
+  CUresult r = fn(m, sizeof(T) == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3,
+                  const_cast<T *>(base), gdim, gstr, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                  CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) {
+    set_last_error("cuTensorMapEncodeTiled failed (" + std::to_string((int)r) + ")");
+    return ELA3D_ERR_CUDA;
+  }
+  return ELA3D_OK;
+}
+
+// -------------------------------------------------------------- engine --
+template <typename T>
+struct Shot {
+  ela3d_params p{};
+  std::vector<int32_t> rec;
+  int px = 0, nsamp = 0;
+  int lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+  char *pool = nullptr;
+  T *prof = nullptr;
+  size_t pool_bytes = 0, prof_bytes = 0;
+  int model_of = -1;   // shot that owns the model arrays (-1: self)
+  ShotDesc<T> d{};
+  ShotMaps maps{};
+  double e_ref = -1.0; // energy monitor reference after the source ended
+};
+
+template <typename T> struct Fp;
+template <> struct Fp<float> {
+  static cudaError_t profile(const AxisProfileArgs &a, float *o, cudaStream_t s) { return launch_profile_f32(a, o, s); }
+  static cudaError_t stf(const StfArgs &a, float *o, cudaStream_t s) { return launch_stf_f32(a, o, s); }
+  static cudaError_t pad(const float *src, float *dst, int nx, int ny, int nz, int px, cudaStream_t s) {
+    return launch_pad_f32(src, dst, nx, ny, nz, px, s);
+  }
+  static cudaError_t explosive(const ShotDesc<float> *d, int n, int tick, cudaStream_t s) {
+    return launch_explosive_f32(d, n, tick, s);
+  }
+  static cudaError_t energy(const ShotDesc<float> *d, int nx, int ny, int nz, double *o, cudaStream_t s) {
+    return launch_energy_f32(d, nx, ny, nz, o, s);
+  }
+};
+template <> struct Fp<double> {
+  static cudaError_t profile(const AxisProfileArgs &a, double *o, cudaStream_t s) { return launch_profile_f64(a, o, s); }
+  static cudaError_t stf(const StfArgs &a, double *o, cudaStream_t s) { return launch_stf_f64(a, o, s); }
+  static cudaError_t pad(const float *src, double *dst, int nx, int ny, int nz, int px, cudaStream_t s) {
+    return launch_pad_f64(src, dst, nx, ny, nz, px, s);
+  }
+  static cudaError_t explosive(const ShotDesc<double> *d, int n, int tick, cudaStream_t s) {
+    return launch_explosive_f64(d, n, tick, s);
+  }
+  static cudaError_t energy(const ShotDesc<double> *d, int nx, int ny, int nz, double *o, cudaStream_t s) {
+    return launch_energy_f64(d, nx, ny, nz, o, s);
+  }
+};
+
+static size_t al256(size_t b) { return (b + 255) & ~size_t(255); }
+
+template <typename T>
+class Engine final : public EngineBase {
+ public:
+  Engine() = default;
+  ~Engine() override { release(); }
+
+  ela3d_status init() {
+    CK(cudaGetDevice(&device_));
+    CK(cudaDeviceGetAttribute(&num_sms_, cudaDevAttrMultiProcessorCount, device_));
+    CK(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
+    CK(cudaMalloc(&d_err_, sizeof(unsigned)));
+    CK(cudaMemset(d_err_, 0, sizeof(unsigned)));
+    CK(cudaMalloc(&d_energy_, sizeof(double)));
+    return ELA3D_OK;
+  }
+
+  int nshots() const override { return (int)shots_.size(); }
+  int steps_done() const override { return tick_; }
+  cudaStream_t stream() const override { return stream_; }
+
+  ela3d_status add_shot(const ela3d_params &p, const float *cp, const float *cs, const float *rho,
+                        int shared_model_of) override {
+    if (finalized_) BAD("engine already finalized");
+    ela3d_status st = validate_params(p);
+    if (st != ELA3D_OK) return st;
+    if ((p.precision == ELA3D_FP64) != (sizeof(T) == 8)) BAD("precision does not match the engine");
+    if (shared_model_of >= (int)shots_.size()) BAD("shared model index out of range");
+    if (shared_model_of >= 0) {
+      const ela3d_params &q = shots_[shared_model_of]->p;
+      if (q.nx != p.nx || q.ny != p.ny || q.nz != p.nz) BAD("shared model needs equal grids");
+      while (shots_[shared_model_of]->model_of >= 0) shared_model_of = shots_[shared_model_of]->model_of;
+    } else if (!cp || !cs || !rho) {
+      BAD("model arrays missing");
+    }
+    auto sh = std::make_unique<Shot<T>>();
+    Shot<T> &s = *sh;
+    s.p = p;
+    s.rec.assign(p.rec, p.rec + 3 * (size_t)p.nrec);
+    s.p.rec = s.rec.data();
+    s.model_of = shared_model_of;
+    const int nx = p.nx, ny = p.ny, nz = p.nz;
+    constexpr int kAlign = 128 / (int)sizeof(T);
+    s.px = (nx + kAlign - 1) / kAlign * kAlign;
+    s.nsamp = p.nstep / p.sampgat;
+    const int px = s.px;
+
+    // 1. C-PML profiles in FP64 on the device (then rounded to T)
+    s.prof_bytes = sizeof(T) * 6 * (size_t)(px + ny + nz);
+    CK(cudaMalloc(&s.prof, s.prof_bytes));
+    const double PI = 3.141592653589793238462643;
+    AxisProfileArgs a{};
+    a.compat = p.pml_mode == ELA3D_PML_COMPAT;
+    a.npml = p.npml;
+    a.ny = ny;
+    a.dy = p.dy;
+    a.npower = p.npower;
+    a.k_max = p.k_max;
+    a.alpha_max = p.alpha_max < 0 ? PI * p.f0 : p.alpha_max;
+    a.rcoef = p.rcoef > 0 ? p.rcoef : 1e-3;
+    a.vpml = p.vpml;
+    a.dt = p.dt;
+    const int ns[3] = {nx, ny, nz}, strides[3] = {px, ny, nz};
+    const double ds[3] = {p.dx, p.dy, p.dz};
+    size_t off[3] = {0, 6 * (size_t)px, 6 * (size_t)(px + ny)};
+    for (int ax = 0; ax < 3; ++ax) {
+      a.axis = ax;
+      a.n = ns[ax];
+      a.stride = strides[ax];
+      a.d = ds[ax];
+      if (p.npml == 0) {  // no layer: identity profiles
+        std::vector<T> id(6 * (size_t)strides[ax]);
+        for (int q = 0; q < 6; ++q)
+          for (int i = 0; i < strides[ax]; ++i) id[(size_t)q * strides[ax] + i] = (q == PR_A || q == PR_AH) ? T(0) : T(1);
+        CK(cudaMemcpyAsync(s.prof + off[ax], id.data(), id.size() * sizeof(T), cudaMemcpyHostToDevice, stream_));
+      } else {
+        CK(Fp<T>::profile(a, s.prof + off[ax], stream_));
+      }
+    }
+    std::vector<T> hprof(6 * (size_t)(px + ny + nz));
+    CK(cudaMemcpyAsync(hprof.data(), s.prof, s.prof_bytes, cudaMemcpyDeviceToHost, stream_));
+    CK(cudaStreamSynchronize(stream_));
+    for (int ax = 0; ax < 3; ++ax) {
+      std::vector<double> af(ns[ax]), ah(ns[ax]);
+      for (int i = 0; i < ns[ax]; ++i) {
+        af[i] = (double)hprof[off[ax] + (size_t)PR_A * strides[ax] + i];
+        ah[i] = (double)hprof[off[ax] + (size_t)PR_AH * strides[ax] + i];
+      }
+      slab_extent(af.data(), ah.data(), ns[ax], &s.lo[ax], &s.hi[ax]);
+    }
+    // x slab boundaries on 16-byte groups
+    constexpr int V = Vec<T>::N;
+    int xl = (s.lo[0] + V - 1) / V * V, xr = s.hi[0] / V * V;
+    if (xl >= xr || s.lo[0] >= nx) { xl = px; xr = px; }
+    int yl = s.lo[1], yr = s.hi[1];
+    int zl = s.lo[2], zr = s.hi[2];
+    const int xw = xl + (px - xr), yw = yl + (ny - yr), zw = zl + (nz - zr);
+
+    // 2. one pool for fields, model, psi slabs, source table, receivers, traces
+    const size_t cells = (size_t)px * ny * nz;
+    const size_t nrec = (size_t)p.nrec;
+    size_t o = 0;
+    auto take = [&](size_t bytes) { size_t at = o; o += al256(bytes); return at; };
+    size_t o_f[9];
+    for (int c = 0; c < 9; ++c) o_f[c] = take(cells * sizeof(T));
+    size_t o_m[3] = {0, 0, 0};
+    if (shared_model_of < 0)
+      for (int c = 0; c < 3; ++c) o_m[c] = take(cells * sizeof(T));
+    const size_t psx = (size_t)nz * ny * xw, psy = (size_t)nz * yw * px, psz = (size_t)zw * ny * px;
+    const size_t o_px = take(6 * psx * sizeof(T)), o_py = take(6 * psy * sizeof(T)), o_pz = take(6 * psz * sizeof(T));
+    const size_t o_stf = take(std::max(1, p.nstep) * sizeof(T));
+    const size_t o_rp = take((size_t)(nz + 1) * sizeof(int));
+    const size_t o_rs = take(std::max<size_t>(1, nrec) * sizeof(int4));
+    const size_t o_seis = take(std::max<size_t>(1, nrec * 3 * s.nsamp) * sizeof(T));
+    s.pool_bytes = o;
+    CK(cudaMalloc(&s.pool, s.pool_bytes));
+    CK(cudaMemsetAsync(s.pool, 0, s.pool_bytes, stream_));
+
+    ShotDesc<T> &d = s.d;
+    d.nx = nx; d.ny = ny; d.nz = nz; d.px = px;
+    d.tick0 = 0;
+    d.nstep = p.nstep;
+    d.xl = xl; d.xr = xr; d.xw = xw;
+    d.yl = yl; d.yr = yr; d.yw = yw;
+    d.zl = zl; d.zr = zr; d.zw = zw;
+    d.src_i = p.src_i; d.src_j = p.src_j; d.src_k = p.src_k; d.src_kind = p.src_kind;
+    d.nrec = p.nrec; d.nsamp = s.nsamp; d.sampgat = p.sampgat;
+    d.dt = (T)p.dt;
+    d.idx = T(1) / (T)p.dx;
+    d.idy = T(1) / (T)p.dy;
+    d.idz = T(1) / (T)p.dz;
+    for (int c = 0; c < 3; ++c) d.src_w[c] = (T)p.src_w[c];
+    const double ang = p.angle_force * PI / 180.0;
+    d.expl_w[0] = (T)std::sin(ang);
+    d.expl_w[1] = (T)std::sin(ang);
+    d.expl_w[2] = (T)std::cos(ang);
+    for (int c = 0; c < 9; ++c) d.f[c] = reinterpret_cast<T *>(s.pool + o_f[c]);
+    if (shared_model_of < 0) {
+      d.cp = reinterpret_cast<T *>(s.pool + o_m[0]);
+      d.cs = reinterpret_cast<T *>(s.pool + o_m[1]);
+      d.rho = reinterpret_cast<T *>(s.pool + o_m[2]);
+    } else {
+      const ShotDesc<T> &od = shots_[shared_model_of]->d;
+      d.cp = od.cp; d.cs = od.cs; d.rho = od.rho;
+    }
+    d.psi_x = reinterpret_cast<T *>(s.pool + o_px);
+    d.psi_y = reinterpret_cast<T *>(s.pool + o_py);
+    d.psi_z = reinterpret_cast<T *>(s.pool + o_pz);
+    d.psx = (long long)psx; d.psy = (long long)psy; d.psz = (long long)psz;
+    d.prof_x = s.prof;
+    d.prof_y = s.prof + off[1];
+    d.prof_z = s.prof + off[2];
+    d.stf = reinterpret_cast<T *>(s.pool + o_stf);
+    d.rec_plane = reinterpret_cast<int *>(s.pool + o_rp);
+    d.rec_sorted = reinterpret_cast<int4 *>(s.pool + o_rs);
+    d.seis = reinterpret_cast<T *>(s.pool + o_seis);
+
+    // 3. model upload into the padded layout
+    if (shared_model_of < 0) {
+      const float *src[3] = {cp, cs, rho};
+      T *dst[3] = {const_cast<T *>(d.cp), const_cast<T *>(d.cs), const_cast<T *>(d.rho)};
+      if (sizeof(T) == 4) {
+        for (int c = 0; c < 3; ++c)
+          CK(cudaMemcpy2DAsync(dst[c], px * sizeof(T), src[c], nx * sizeof(float), nx * sizeof(float),
+                               (size_t)ny * nz, cudaMemcpyHostToDevice, stream_));
+      } else {
+        float *stage = nullptr;
+        CK(cudaMalloc(&stage, (size_t)nx * ny * nz * sizeof(float)));
+        for (int c = 0; c < 3; ++c) {
+          CK(cudaMemcpyAsync(stage, src[c], (size_t)nx * ny * nz * sizeof(float), cudaMemcpyHostToDevice, stream_));
+          CK(Fp<T>::pad(stage, dst[c], nx, ny, nz, px, stream_));
+        }
+        CK(cudaStreamSynchronize(stream_));
+        CK(cudaFree(stage));
+      }
+    }
+    // 4. source time function (FP64 on the device)
+    if (p.nstep > 0) {
+      StfArgs sa{p.nstep, p.stf, p.f0, p.t0, p.factor, p.dt};
+      CK(Fp<T>::stf(sa, const_cast<T *>(d.stf), stream_));
+    }
+    // 5. receivers sorted by (k, j, i) with a per-plane index
+    {
+      std::vector<int4> rs(nrec);
+      for (size_t r = 0; r < nrec; ++r) rs[r] = make_int4(s.rec[3 * r], s.rec[3 * r + 1], s.rec[3 * r + 2], (int)r);
+      std::sort(rs.begin(), rs.end(), [](const int4 &u, const int4 &v) {
+        if (u.z != v.z) return u.z < v.z;
+        if (u.y != v.y) return u.y < v.y;
+        if (u.x != v.x) return u.x < v.x;
+        return u.w < v.w;
+      });
+      std::vector<int> rp(nz + 1, 0);
+      for (size_t r = 0; r < nrec; ++r) rp[rs[r].z + 1]++;
+      for (int k = 0; k < nz; ++k) rp[k + 1] += rp[k];
+      CK(cudaMemcpyAsync(const_cast<int *>(d.rec_plane), rp.data(), rp.size() * sizeof(int), cudaMemcpyHostToDevice,
+                         stream_));
+      if (nrec)
+        CK(cudaMemcpyAsync(const_cast<int4 *>(d.rec_sorted), rs.data(), nrec * sizeof(int4), cudaMemcpyHostToDevice,
+                           stream_));
+      CK(cudaStreamSynchronize(stream_));
+    }
+    if (p.src_kind == ELA3D_SRC_EXPLOSIVE) any_explosive_ = true;
+    shots_.push_back(std::move(sh));
+    return ELA3D_OK;
+  }
+
+  ela3d_status finalize(const TuneChoice *choice) override {
+    if (finalized_) return ELA3D_OK;
+    if (shots_.empty()) BAD("no shots");
+    int nv = 0;
+    const Variant *vs = variants(&nv);
+    TuneChoice c = choice ? *choice : default_choice(sizeof(T) == 8, shots_[0]->p.nx, shots_[0]->p.ny, shots_[0]->p.nz);
+    if (c.variant < 0 || c.variant >= nv || vs[c.variant].fp64 != (sizeof(T) == 8)) BAD("bad kernel variant");
+    var_ = &vs[c.variant];
+    choice_ = c;
+    const int TX = var_->tx, TY = var_->ty, H = var_->halo;
+    std::vector<ShotShape> shapes;
+    for (auto &sp : shots_) {
+      Shot<T> &s = *sp;
+      ShotDesc<T> &d = s.d;
+      const int nx = d.nx, ny = d.ny, nz = d.nz, px = d.px;
+      CUtensorMap *m = s.maps.stress;
+      ela3d_status st;
+#define ENC(map, ptr, bw, bh) \
+  if ((st = encode_map<T>(map, ptr, nx, ny, nz, px, bw, bh)) != ELA3D_OK) return st
+      ENC(&m[0], d.f[0], TX + H, TY + 1);
+      ENC(&m[1], d.f[1], TX + H, TY + 1);
+      ENC(&m[2], d.f[2], TX + H, TY + 1);
+      ENC(&m[3], d.cs, TX + H, TY + 1);
+      ENC(&m[4], d.rho, TX + H, TY + 1);
+      ENC(&m[5], d.cp, TX, TY);
+      for (int q = 0; q < 6; ++q) ENC(&m[6 + q], d.f[3 + q], TX, TY);
+      CUtensorMap *v = s.maps.vel;
+      ENC(&v[0], d.f[3], TX + H, TY);      // sxx
+      ENC(&v[1], d.f[4], TX, TY + 1);      // syy
+      ENC(&v[2], d.f[5], TX, TY);          // szz
+      ENC(&v[3], d.f[6], TX + H, TY + 1);  // sxy
+      ENC(&v[4], d.f[7], TX + H, TY);      // sxz
+      ENC(&v[5], d.f[8], TX, TY + 1);      // syz
+      ENC(&v[6], d.rho, TX + H, TY + 1);   // rho
+      for (int q = 0; q < 3; ++q) ENC(&v[7 + q], d.f[q], TX, TY);
+#undef ENC
+      shapes.push_back({nx, ny, nz});
+    }
+    CK(cudaFuncSetAttribute(var_->stress, cudaFuncAttributeMaxDynamicSharedMemorySize, var_->stress_smem));
+    CK(cudaFuncSetAttribute(var_->velocity, cudaFuncAttributeMaxDynamicSharedMemorySize, var_->vel_smem));
+    int occ_s = 0, occ_v = 0;
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_s, var_->stress, var_->threads, var_->stress_smem));
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_v, var_->velocity, var_->threads, var_->vel_smem));
+    int per_sm = std::max(1, std::min(occ_s, occ_v));
+    if (c.blocks_per_sm > 0) per_sm = std::min(per_sm, c.blocks_per_sm);
+    std::vector<Item> items;
+    std::vector<int2> ranges;
+    build_schedule(shapes, TX, TY, c.kind, c.chunk, per_sm * num_sms_, &items, &ranges);
+    if (items.empty()) BAD("empty schedule");
+    for (const Item &it : items)
+      if (it.k1 <= it.k0) BAD("internal: empty work item");
+    nblocks_ = (int)ranges.size();
+    std::vector<ShotDesc<T>> descs;
+    std::vector<ShotMaps> maps;
+    for (auto &sp : shots_) { descs.push_back(sp->d); maps.push_back(sp->maps); }
+    CK(cudaMalloc(&d_desc_, descs.size() * sizeof(ShotDesc<T>)));
+    CK(cudaMalloc(&d_maps_, maps.size() * sizeof(ShotMaps)));
+    CK(cudaMalloc(&d_items_, items.size() * sizeof(Item)));
+    CK(cudaMalloc(&d_ranges_, ranges.size() * sizeof(int2)));
+    CK(cudaMemcpyAsync(d_desc_, descs.data(), descs.size() * sizeof(ShotDesc<T>), cudaMemcpyHostToDevice, stream_));
+    CK(cudaMemcpyAsync(d_maps_, maps.data(), maps.size() * sizeof(ShotMaps), cudaMemcpyHostToDevice, stream_));
+    CK(cudaMemcpyAsync(d_items_, items.data(), items.size() * sizeof(Item), cudaMemcpyHostToDevice, stream_));
+    CK(cudaMemcpyAsync(d_ranges_, ranges.data(), ranges.size() * sizeof(int2), cudaMemcpyHostToDevice, stream_));
+    CK(cudaStreamSynchronize(stream_));
+    finalized_ = true;
+    return ELA3D_OK;
+  }
+
+  ela3d_status launch_step(int tick) {
+    void *args[] = {&d_desc_, &d_maps_, &d_items_, &d_ranges_, &tick, &d_err_};
+    cudaEvent_t e0 = nullptr, e1 = nullptr, e2 = nullptr;
+    if (timing_) {
+      e0 = event(); e1 = event(); e2 = event();
+      CK(cudaEventRecord(e0, stream_));
+    }
+    CK(cudaLaunchKernel(var_->stress, dim3(nblocks_), dim3(var_->threads), args, var_->stress_smem, stream_));
+    if (timing_) CK(cudaEventRecord(e1, stream_));
+    CK(cudaLaunchKernel(var_->velocity, dim3(nblocks_), dim3(var_->threads), args, var_->vel_smem, stream_));
+    if (timing_) {
+      CK(cudaEventRecord(e2, stream_));
+      pending_.push_back({e0, e1, e2});
+    }
+    if (any_explosive_) CK(Fp<T>::explosive(d_desc_, (int)shots_.size(), tick, stream_));
+    return ELA3D_OK;
+  }
+
+  ela3d_status enqueue(int nsteps) override {
+    if (!finalized_) BAD("engine not finalized");
+    if (nsteps < 0) BAD("nsteps must be >= 0");
+    for (int s = 0; s < nsteps; ++s) {
+      ela3d_status st = launch_step(tick_ + 1);
+      if (st != ELA3D_OK) return st;
+      ++tick_;
+    }
+    return ELA3D_OK;
+  }
+
+  ela3d_status sync() override {
+    CK(cudaStreamSynchronize(stream_));
+    unsigned err = 0;
+    CK(cudaMemcpy(&err, d_err_, sizeof(unsigned), cudaMemcpyDeviceToHost));
+    collect_timing();
+    if (err) {
+      CK(cudaMemset(d_err_, 0, sizeof(unsigned)));
+      set_last_error("device-side wait exceeded its limit (error bits " + std::to_string(err) + ")");
+      return ELA3D_ERR_TIMEOUT;
+    }
+    return ELA3D_OK;
+  }
+
+  ela3d_status seismograms(int shot, void *out, int out_fp64) override {
+    if (shot < 0 || shot >= nshots() || !out) BAD("bad shot or output");
+    const Shot<T> &s = *shots_[shot];
+    const size_t n = (size_t)s.p.nrec * 3 * s.nsamp;
+    if (n == 0) return ELA3D_OK;
+    std::vector<T> h(n);
+    CK(cudaMemcpyAsync(h.data(), s.d.seis, n * sizeof(T), cudaMemcpyDeviceToHost, stream_));
+    CK(cudaStreamSynchronize(stream_));
+    convert_out(h.data(), n, out, out_fp64);
+    return ELA3D_OK;
+  }
+
+  ela3d_status field(int shot, int comp, void *out, int out_fp64) override {
+    if (shot < 0 || shot >= nshots() || !out) BAD("bad shot or output");
+    if (comp < 0 || comp > 8) BAD("bad field component");
+    const Shot<T> &s = *shots_[shot];
+    const int nx = s.d.nx, ny = s.d.ny, nz = s.d.nz;
+    const size_t n = (size_t)nx * ny * nz;
+    if ((sizeof(T) == 8) == (out_fp64 != 0)) {
+      CK(cudaMemcpy2DAsync(out, nx * sizeof(T), s.d.f[comp], s.d.px * sizeof(T), nx * sizeof(T), (size_t)ny * nz,
+                           cudaMemcpyDeviceToHost, stream_));
+      CK(cudaStreamSynchronize(stream_));
+      return ELA3D_OK;
+    }
+    std::vector<T> h(n);
+    CK(cudaMemcpy2DAsync(h.data(), nx * sizeof(T), s.d.f[comp], s.d.px * sizeof(T), nx * sizeof(T), (size_t)ny * nz,
+                         cudaMemcpyDeviceToHost, stream_));
+    CK(cudaStreamSynchronize(stream_));
+    convert_out(h.data(), n, out, out_fp64);
+    return ELA3D_OK;
+  }
+
+  ela3d_status energy(int shot, double *out) override {
+    if (shot < 0 || shot >= nshots() || !out) BAD("bad shot or output");
+    const Shot<T> &s = *shots_[shot];
+    CK(cudaMemsetAsync(d_energy_, 0, sizeof(double), stream_));
+    const ShotDesc<T> *dd = d_desc_ ? d_desc_ + shot : nullptr;
+    if (!dd) BAD("engine not finalized");
+    CK(Fp<T>::energy(dd, s.d.nx, s.d.ny, s.d.nz, d_energy_, stream_));
+    CK(cudaMemcpyAsync(out, d_energy_, sizeof(double), cudaMemcpyDeviceToHost, stream_));
+    CK(cudaStreamSynchronize(stream_));
+    return ELA3D_OK;
+  }
+
+  ela3d_status info(int shot, ela3d_plan_info *out) override {
+    if (shot < 0 || shot >= nshots() || !out) BAD("bad shot or output");
+    const Shot<T> &s = *shots_[shot];
+    out->nx = s.d.nx; out->ny = s.d.ny; out->nz = s.d.nz; out->pitch_x = s.d.px;
+    out->step = tick_ - s.d.tick0;
+    out->nsamp = s.nsamp;
+    out->nrec = s.p.nrec;
+    out->precision = sizeof(T) == 8 ? ELA3D_FP64 : ELA3D_FP32;
+    out->device_bytes = (int64_t)(s.pool_bytes + s.prof_bytes);
+    for (int a = 0; a < 3; ++a) { out->slab_lo[a] = s.lo[a]; out->slab_hi[a] = s.hi[a]; }
+    return ELA3D_OK;
+  }
+
+  ela3d_status set_timing(bool on) override {
+    timing_ = on;
+    if (on) { t_stress_ = t_vel_ = 0.0; n_stress_ = n_vel_ = 0; }
+    return ELA3D_OK;
+  }
+
+  ela3d_status timing(double *s_ms, double *v_ms, int64_t *ns, int64_t *nv) override {
+    CK(cudaStreamSynchronize(stream_));
+    collect_timing();
+    if (s_ms) *s_ms = t_stress_;
+    if (v_ms) *v_ms = t_vel_;
+    if (ns) *ns = n_stress_;
+    if (nv) *nv = n_vel_;
+    return ELA3D_OK;
+  }
+
+  // stability monitor for one shot (called by the plan between chunks)
+  ela3d_status check_energy(int shot) {
+    double e = 0.0;
+    ela3d_status st = energy(shot, &e);
+    if (st != ELA3D_OK) return st;
+    Shot<T> &s = *shots_[shot];
+    if (!std::isfinite(e)) {
+      set_last_error("energy is not finite");
+      return ELA3D_ERR_UNSTABLE;
+    }
+    const double t = (tick_ - s.d.tick0) * s.p.dt;
+    if (t > 2.5 * s.p.t0 + 2.0 / std::max(1e-30, s.p.f0)) {  // the source has ended
+      if (s.e_ref < 0) s.e_ref = e;
+      else if (e > 2.0 * s.e_ref + 1e-300) {
+        set_last_error("energy grew after the source ended");
+        return ELA3D_ERR_UNSTABLE;
+      }
+    }
+    return ELA3D_OK;
+  }
+  const ela3d_params &params(int shot) const { return shots_[shot]->p; }
+
+ private:
+  template <typename U>
+  static void convert_out(const U *h, size_t n, void *out, int out_fp64) {
+    if (out_fp64) {
+      double *o = static_cast<double *>(out);
+      for (size_t i = 0; i < n; ++i) o[i] = (double)h[i];
+    } else {
+      float *o = static_cast<float *>(out);
+      for (size_t i = 0; i < n; ++i) o[i] = (float)h[i];
+    }
+  }
+
+  cudaEvent_t event() {
+    cudaEvent_t e = nullptr;
+    if (!free_events_.empty()) {
+      e = free_events_.back();
+      free_events_.pop_back();
+    } else {
+      cudaEventCreate(&e);
+    }
+    return e;
+  }
+
+  void collect_timing() {
+    for (auto &t : pending_) {
+      float a = 0.f, b = 0.f;
+      if (cudaEventElapsedTime(&a, t.e0, t.e1) == cudaSuccess) { t_stress_ += a; ++n_stress_; }
+      if (cudaEventElapsedTime(&b, t.e1, t.e2) == cudaSuccess) { t_vel_ += b; ++n_vel_; }
+      free_events_.push_back(t.e0);
+      free_events_.push_back(t.e1);
+      free_events_.push_back(t.e2);
+    }
+    pending_.clear();
+  }
+
+  void release() {
+    if (stream_) cudaStreamSynchronize(stream_);
+    for (auto &sp : shots_) {
+      if (sp->pool) cudaFree(sp->pool);
+      if (sp->prof) cudaFree(sp->prof);
+    }
+    shots_.clear();
+    for (auto &t : pending_) { cudaEventDestroy(t.e0); cudaEventDestroy(t.e1); cudaEventDestroy(t.e2); }
+    for (auto e : free_events_) cudaEventDestroy(e);
+    pending_.clear();
+    free_events_.clear();
+    if (d_desc_) cudaFree(d_desc_);
+    if (d_maps_) cudaFree(d_maps_);
+    if (d_items_) cudaFree(d_items_);
+    if (d_ranges_) cudaFree(d_ranges_);
+    if (d_err_) cudaFree(d_err_);
+    if (d_energy_) cudaFree(d_energy_);
+    if (stream_) cudaStreamDestroy(stream_);
+    d_desc_ = nullptr; d_maps_ = nullptr; d_items_ = nullptr; d_ranges_ = nullptr;
+    d_err_ = nullptr; d_energy_ = nullptr; stream_ = nullptr;
+  }
+
+  struct Ev { cudaEvent_t e0, e1, e2; };
+  int device_ = 0, num_sms_ = 1;
+  cudaStream_t stream_ = nullptr;
+  std::vector<std::unique_ptr<Shot<T>>> shots_;
+  const Variant *var_ = nullptr;
+  TuneChoice choice_{};
+  bool finalized_ = false, any_explosive_ = false;
+  ShotDesc<T> *d_desc_ = nullptr;
+  ShotMaps *d_maps_ = nullptr;
+  Item *d_items_ = nullptr;
+  int2 *d_ranges_ = nullptr;
+  unsigned *d_err_ = nullptr;
+  double *d_energy_ = nullptr;
+  int nblocks_ = 0;
+  int tick_ = 0;
+  bool timing_ = false;
+  std::vector<Ev> pending_;
+  std::vector<cudaEvent_t> free_events_;
+  double t_stress_ = 0.0, t_vel_ = 0.0;
+  int64_t n_stress_ = 0, n_vel_ = 0;
+
+};
+
+std::unique_ptr<EngineBase> make_engine(int fp64, ela3d_status *st) {
+  std::unique_ptr<EngineBase> e;
+  if (fp64) {
+    auto p = std::make_unique<Engine<double>>();
+    *st = p->init();
+    e = std::move(p);
+  } else {
+    auto p = std::make_unique<Engine<float>>();
+    *st = p->init();
+    e = std::move(p);
+  }
+  return e;
+}
+
+ela3d_status engine_check_energy(EngineBase *e, int shot, int fp64) {
+  if (fp64) return static_cast<Engine<double> *>(e)->check_energy(shot);
+  return static_cast<Engine<float> *>(e)->check_energy(shot);
+}
+
+}  // namespace ela3d

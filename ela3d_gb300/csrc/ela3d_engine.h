@@ -1,0 +1,75 @@
+// ela3d_engine.h -- host engine: a set of shots resident on one GPU,
+// advanced together by the two stencil kernels (one launch per half-step).
+// A single-shot plan is an engine with one shot; the batch and the server
+// build on the same class.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/ela3d.h"
+#include "ela3d_internal.h"
+
+namespace ela3d {
+
+void set_last_error(const std::string &msg);
+const char *last_error();
+ela3d_status status_from_cuda(cudaError_t e, const char *what);
+
+// Validates a parameter block (grid, spacing, source, receivers).
+ela3d_status validate_params(const ela3d_params &p);
+
+// Slab extents of one axis from its profile arrays: cells [0, lo) and
+// [hi, n) may have a != 0; every cell in [lo, hi) has a == 0 in both the
+// full and the half profile.  Returns lo == hi == n when the layer covers
+// everything.  (Host logic, unit-tested without a GPU.)
+void slab_extent(const double *a_full, const double *a_half, int n, int *lo, int *hi);
+
+// Work schedule.  Units are (shot, tile, plane); kind 0 gives every block a
+// contiguous, equal share of the units in (shot, tile, plane) order; kind 1
+// splits each tile column into z-chunks of `chunk` planes and deals the
+// chunks round-robin in (shot, chunk, tile) order so that blocks running at
+// the same time work on neighbouring tiles.
+struct ShotShape {
+  int nx, ny, nz;
+};
+void build_schedule(const std::vector<ShotShape> &shots, int tx, int ty, int kind, int chunk,
+                    int max_blocks, std::vector<Item> *items, std::vector<int2> *ranges);
+
+// Chooses the kernel variant for a grid: the measured autotuner table when
+// one was loaded, else a fixed default per precision.
+struct TuneChoice {
+  int variant;     // index into variants()
+  int kind, chunk; // schedule
+  int blocks_per_sm;  // 0 = occupancy limit
+};
+TuneChoice default_choice(int fp64, int nx, int ny, int nz);
+
+class EngineBase {
+ public:
+  virtual ~EngineBase() = default;
+  virtual ela3d_status add_shot(const ela3d_params &p, const float *cp, const float *cs, const float *rho,
+                                int shared_model_of) = 0;
+  virtual ela3d_status finalize(const TuneChoice *choice) = 0;
+  virtual ela3d_status enqueue(int nsteps) = 0;
+  virtual ela3d_status sync() = 0;
+  virtual ela3d_status seismograms(int shot, void *out, int out_fp64) = 0;
+  virtual ela3d_status field(int shot, int comp, void *out, int out_fp64) = 0;
+  virtual ela3d_status energy(int shot, double *out) = 0;
+  virtual ela3d_status info(int shot, ela3d_plan_info *out) = 0;
+  virtual ela3d_status set_timing(bool on) = 0;
+  virtual ela3d_status timing(double *s_ms, double *v_ms, int64_t *ns, int64_t *nv) = 0;
+  virtual int nshots() const = 0;
+  virtual int steps_done() const = 0;
+  virtual cudaStream_t stream() const = 0;
+};
+
+std::unique_ptr<EngineBase> make_engine(int fp64, ela3d_status *st);
+
+// Energy-based stability check of one shot (ELA3D_ERR_UNSTABLE on failure).
+ela3d_status engine_check_energy(EngineBase *e, int shot, int fp64);
+
+}  // namespace ela3d

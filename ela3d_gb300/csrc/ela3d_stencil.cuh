@@ -1,0 +1,725 @@
+// ela3d_stencil.cuh -- the two time-loop kernels: stress half-step and
+// velocity half-step, templated on the real type and the x-y tile.
+//
+// Scheme (2.5-D z-march, one launch per half-step):
+//  - a block owns a list of work items (shot, x-y tile, z-run [k0, k1));
+//  - for each plane k of an item, one elected thread issues TMA tiled loads
+//    of every input array's x-y tile (with the one-cell halos the stencil
+//    needs) into a ring of NS shared-memory stages, completing on an
+//    mbarrier per stage; out-of-grid halo cells arrive as zeros (the TMA
+//    fill), which is also the zero plane above k = nz-1 that the reference's
+//    sigma_xz/sigma_yz loop reads (simpelmodel.cpp:450,477);
+//  - the block computes plane k from stages k and k+1 (the z+1 neighbours)
+//    and keeps the z-1 neighbours in registers, each thread owning 16 bytes
+//    of consecutive x cells of one row (float4 / double2 accesses);
+//  - C-PML memory variables are read and written only in the PML slabs;
+//  - cells outside the update ranges of the reference's loops keep their
+//    value (the Dirichlet edges), receivers are sampled after the velocity
+//    update and the force source is added after that (simpelmodel.cpp:592-622).
+#pragma once
+
+#include "ela3d_device.cuh"
+
+namespace ela3d {
+
+template <typename T, int TX_, int TY_, int NS_>
+struct Geo {
+  static constexpr int VEC = Vec<T>::N;  // cells per thread (16 bytes)
+  static constexpr int H = VEC;          // halo width in x (16 bytes, the TMA x alignment)
+  static constexpr int TX = TX_, TY = TY_, NS = NS_;
+  static constexpr int NTX = TX / VEC;
+  static constexpr int NT = NTX * TY;
+  static constexpr int WW = TX + H;
+  static_assert(TX % VEC == 0 && TX + H <= 256 && TY + 1 <= 256, "tile shape");
+  __host__ __device__ static constexpr int al(int b) { return (b + 127) & ~127; }
+  static constexpr int C = TX * TY;          // center box
+  static constexpr int W1 = WW * (TY + 1);   // wide box with one extra row
+  static constexpr int W0 = WW * TY;         // wide box
+  static constexpr int Y1 = TX * (TY + 1);   // narrow box with one extra row
+  __host__ __device__ static constexpr int sz(int e) { return al(e * (int)sizeof(T)); }
+  static constexpr int SC = (C * (int)sizeof(T) + 127) & ~127;  // bytes of a centre box
+  // stress stage: vx vy vz cs rho (W1), cp s0..s5 (C)
+  static constexpr int S_VX = 0;
+  static constexpr int S_VY = S_VX + sz(W1);
+  static constexpr int S_VZ = S_VY + sz(W1);
+  static constexpr int S_CS = S_VZ + sz(W1);
+  static constexpr int S_RHO = S_CS + sz(W1);
+  static constexpr int S_CP = S_RHO + sz(W1);
+  static constexpr int S_SIG = S_CP + sz(C);  // six centre boxes follow
+  static constexpr int S_STAGE = S_SIG + 6 * sz(C);
+  static constexpr int S_TX = (int)sizeof(T) * (5 * W1 + 7 * C);
+  // velocity stage
+  static constexpr int V_SXX = 0;                 // W0
+  static constexpr int V_SYY = V_SXX + sz(W0);    // Y1
+  static constexpr int V_SZZ = V_SYY + sz(Y1);    // C
+  static constexpr int V_SXY = V_SZZ + sz(C);     // W1
+  static constexpr int V_SXZ = V_SXY + sz(W1);    // W0
+  static constexpr int V_SYZ = V_SXZ + sz(W0);    // Y1
+  static constexpr int V_RHO = V_SYZ + sz(Y1);    // W1
+  static constexpr int V_V = V_RHO + sz(W1);      // vx vy vz (C)
+  static constexpr int V_STAGE = V_V + 3 * sz(C);
+  static constexpr int V_TX = (int)sizeof(T) * (2 * W0 + 2 * Y1 + 4 * C + 2 * W1);
+  // mbarriers live after the stages, so the TMA destinations start at the
+  // (aligned) base of the block's dynamic shared memory
+  static constexpr int S_SMEM = NS * S_STAGE + 8 * NS;
+  static constexpr int V_SMEM = NS * V_STAGE + 8 * NS;
+};
+
+// Producer/consumer bookkeeping of the load sequence.  Every thread runs it
+// (it is a few integer operations per plane); thread 0 also issues the TMA.
+// Loads are numbered n = 0, 1, ...; load n goes to stage n % NS and its
+// mbarrier phase parity is (n / NS) & 1.  Item i contributes loads for
+// planes k0 .. k1 (k1 is the look-ahead plane, possibly nz = all zeros).
+struct LoadCursor {
+  int item, k;     // next plane to load
+  int end;         // item range end
+  long long n;     // loads issued
+};
+
+template <typename T>
+__device__ __forceinline__ int tiles_x_of(const ShotDesc<T> &s, int TX) {
+  return (s.nx + TX - 1) / TX;
+}
+
+// ----------------------------------------------------------- stress ----
+template <typename T, int TX, int TY, int NS>
+__global__ void __launch_bounds__(Geo<T, TX, TY, NS>::NT)
+    stress_kernel(const ShotDesc<T> *__restrict__ shots, const ShotMaps *__restrict__ maps,
+                  const Item *__restrict__ items, const int2 *__restrict__ ranges, int tick,
+                  unsigned *__restrict__ err) {
+  using G = Geo<T, TX, TY, NS>;
+  constexpr int V = G::VEC, H = G::H, WW = G::WW;
+  extern __shared__ __align__(1024) unsigned char smem[];
+  uint64_t *full = reinterpret_cast<uint64_t *>(smem + NS * G::S_STAGE);
+
+  const int tid = threadIdx.x;
+  const int tx = tid % G::NTX, ty = tid / G::NTX;
+  const int2 range = ranges[blockIdx.x];
+  if (range.x >= range.y) return;
+
+  if (tid == 0) {
+    for (int s = 0; s < NS; ++s) mbar_init(&full[s], 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+
+  LoadCursor pc{range.x, items[range.x].k0, range.y, 0};
+  auto issue = [&](bool do_copy) {
+    const Item it = items[pc.item];
+    const int txs = tiles_x_of(shots[it.shot], TX);
+    const int x0 = (it.tile % txs) * TX, y0 = (it.tile / txs) * TY;
+    const int slot = (int)(pc.n % NS);
+    if (do_copy) {
+      unsigned char *st = smem + slot * G::S_STAGE;
+      const CUtensorMap *m = maps[it.shot].stress;
+      uint64_t *bar = &full[slot];
+      mbar_arrive_expect_tx(bar, G::S_TX);
+      tma_load_3d(st + G::S_VX, &m[0], x0, y0, pc.k, bar);
+      tma_load_3d(st + G::S_VY, &m[1], x0 - H, y0 - 1, pc.k, bar);
+      tma_load_3d(st + G::S_VZ, &m[2], x0 - H, y0, pc.k, bar);
+      tma_load_3d(st + G::S_CS, &m[3], x0 - H, y0, pc.k, bar);
+      tma_load_3d(st + G::S_RHO, &m[4], x0 - H, y0, pc.k, bar);
+      tma_load_3d(st + G::S_CP, &m[5], x0, y0, pc.k, bar);
+#pragma unroll
+      for (int c = 0; c < 6; ++c)
+        tma_load_3d(st + G::S_SIG + c * G::SC, &m[6 + c], x0, y0, pc.k, bar);
+    }
+    ++pc.n;
+    if (++pc.k > it.k1) {
+      if (++pc.item < pc.end) pc.k = items[pc.item].k0;
+    }
+  };
+  for (int s = 0; s < NS && pc.item < pc.end; ++s) issue(tid == 0);
+
+  long long consumed = 0;
+  bool timed_out = false;
+
+  for (int ii = range.x; ii < range.y; ++ii) {
+    const Item item = items[ii];
+    const ShotDesc<T> &sd = shots[item.shot];
+    const int nx = sd.nx, ny = sd.ny, nz = sd.nz, px = sd.px;
+    const int txs = tiles_x_of(sd, TX);
+    const int x0 = (item.tile % txs) * TX, y0 = (item.tile / txs) * TY;
+    const int xg = x0 + tx * V, y = y0 + ty;
+    const bool live = (xg < nx) && (y < ny);
+    const T dt = sd.dt, idx = sd.idx, idy = sd.idy, idz = sd.idz;
+    const long long plane = (long long)ny * px;
+
+    // z-1 neighbour of vz for the first plane of the run
+    T vz_zm[V];
+#pragma unroll
+    for (int e = 0; e < V; ++e) vz_zm[e] = T(0);
+    if (live && item.k0 > 0) ld_vec_rw(sd.f[2] + (long long)(item.k0 - 1) * plane + (long long)y * px + xg, vz_zm);
+
+    // x-slab profile and placement (fixed over the run)
+    const bool in_x = live && (xg < sd.xl || xg >= sd.xr);
+    const int xs = xg < sd.xl ? xg : sd.xl + (xg - sd.xr);
+    T ax[V], bx[V], ikx[V], axh[V], bxh[V], ikxh[V];
+    if (in_x) {
+      ld_vec_global(sd.prof_x + PR_A * px + xg, ax);
+      ld_vec_global(sd.prof_x + PR_B * px + xg, bx);
+      ld_vec_global(sd.prof_x + PR_IK * px + xg, ikx);
+      ld_vec_global(sd.prof_x + PR_AH * px + xg, axh);
+      ld_vec_global(sd.prof_x + PR_BH * px + xg, bxh);
+      ld_vec_global(sd.prof_x + PR_IKH * px + xg, ikxh);
+    } else {
+#pragma unroll
+      for (int e = 0; e < V; ++e) { ax[e] = axh[e] = T(0); bx[e] = bxh[e] = ikx[e] = ikxh[e] = T(1); }
+    }
+    const bool in_y = live && (y < sd.yl || y >= sd.yr);
+    const int ys = y < sd.yl ? y : sd.yl + (y - sd.yr);
+    T ay = 0, by = 1, iky = 1, ayh = 0, byh = 1, ikyh = 1;
+    if (in_y) {
+      ay = sd.prof_y[PR_A * ny + y]; by = sd.prof_y[PR_B * ny + y]; iky = sd.prof_y[PR_IK * ny + y];
+      ayh = sd.prof_y[PR_AH * ny + y]; byh = sd.prof_y[PR_BH * ny + y]; ikyh = sd.prof_y[PR_IKH * ny + y];
+    }
+    const int sb = (ty * WW + tx * V);       // vx box (origin x0, y0)
+    const int sl = (ty * WW + H + tx * V);   // vz/cs/rho boxes (origin x0-H, y0)
+    const int syl = sl + WW;                 // vy box (origin x0-H, y0-1): own row is ty+1
+    const int sc = ty * TX + tx * V;         // centre boxes
+
+    for (int k = item.k0; k < item.k1; ++k) {
+      const long long n = consumed;
+      const int s0 = (int)(n % NS), s1 = (int)((n + 1) % NS);
+      bool ok = mbar_wait_bounded(&full[s0], (uint32_t)((n / NS) & 1));
+      ok = ok && mbar_wait_bounded(&full[s1], (uint32_t)(((n + 1) / NS) & 1));
+      timed_out |= !ok;
+      const unsigned char *cur = smem + s0 * G::S_STAGE;
+      const unsigned char *nxt = smem + s1 * G::S_STAGE;
+      const T *bvx = reinterpret_cast<const T *>(cur + G::S_VX);
+      const T *bvy = reinterpret_cast<const T *>(cur + G::S_VY);
+      const T *bvz = reinterpret_cast<const T *>(cur + G::S_VZ);
+      const T *bcs = reinterpret_cast<const T *>(cur + G::S_CS);
+      const T *brho = reinterpret_cast<const T *>(cur + G::S_RHO);
+      const T *bcp = reinterpret_cast<const T *>(cur + G::S_CP);
+      const T *bsig = reinterpret_cast<const T *>(cur + G::S_SIG);
+
+      T vx_c[V], vx_yp[V], vx_zp[V], vy_c[V], vy_ym[V], vy_zp[V], vz_c[V], vz_yp[V];
+      T cs_c[V], cs_yp[V], cs_zp[V], rho_c[V], rho_yp[V], rho_zp[V], cp_c[V];
+      ld_vec(bvx + sb, vx_c);
+      ld_vec(bvx + sb + WW, vx_yp);
+      const T vx_e = bvx[sb + V];
+      ld_vec(reinterpret_cast<const T *>(nxt + G::S_VX) + sb, vx_zp);
+      ld_vec(bvy + syl, vy_c);
+      ld_vec(bvy + syl - WW, vy_ym);
+      const T vy_w = bvy[syl - 1];
+      ld_vec(reinterpret_cast<const T *>(nxt + G::S_VY) + syl, vy_zp);
+      ld_vec(bvz + sl, vz_c);
+      ld_vec(bvz + sl + WW, vz_yp);
+      const T vz_w = bvz[sl - 1];
+      ld_vec(bcs + sl, cs_c);
+      ld_vec(bcs + sl + WW, cs_yp);
+      const T cs_w = bcs[sl - 1];
+      ld_vec(reinterpret_cast<const T *>(nxt + G::S_CS) + sl, cs_zp);
+      ld_vec(brho + sl, rho_c);
+      ld_vec(brho + sl + WW, rho_yp);
+      const T rho_w = brho[sl - 1];
+      ld_vec(reinterpret_cast<const T *>(nxt + G::S_RHO) + sl, rho_zp);
+      ld_vec(bcp + sc, cp_c);
+      T sxx[V], syy[V], szz[V], sxy[V], sxz[V], syz[V];
+      ld_vec(bsig + 0 * (G::SC / (int)sizeof(T)) + sc, sxx);
+      ld_vec(bsig + 1 * (G::SC / (int)sizeof(T)) + sc, syy);
+      ld_vec(bsig + 2 * (G::SC / (int)sizeof(T)) + sc, szz);
+      ld_vec(bsig + 3 * (G::SC / (int)sizeof(T)) + sc, sxy);
+      ld_vec(bsig + 4 * (G::SC / (int)sizeof(T)) + sc, sxz);
+      ld_vec(bsig + 5 * (G::SC / (int)sizeof(T)) + sc, syz);
+
+      const bool in_z = live && (k < sd.zl || k >= sd.zr);
+      const int zs = k < sd.zl ? k : sd.zl + (k - sd.zr);
+      T az = 0, bz = 1, ikz = 1, azh = 0, bzh = 1, ikzh = 1;
+      if (in_z) {
+        az = sd.prof_z[PR_A * nz + k]; bz = sd.prof_z[PR_B * nz + k]; ikz = sd.prof_z[PR_IK * nz + k];
+        azh = sd.prof_z[PR_AH * nz + k]; bzh = sd.prof_z[PR_BH * nz + k]; ikzh = sd.prof_z[PR_IKH * nz + k];
+      }
+      // psi of this group (zero when outside a slab)
+      T px0[V], px1[V], px2[V], py0[V], py1[V], py2[V], pz0[V], pz1[V], pz2[V];
+      T *gx = nullptr, *gy = nullptr, *gz = nullptr;
+      if (in_x) {
+        gx = sd.psi_x + ((long long)k * ny + y) * sd.xw + xs;
+        ld_vec_rw(gx + PSI_S0 * sd.psx, px0);
+        ld_vec_rw(gx + PSI_S1 * sd.psx, px1);
+        ld_vec_rw(gx + PSI_S2 * sd.psx, px2);
+      } else {
+#pragma unroll
+        for (int e = 0; e < V; ++e) px0[e] = px1[e] = px2[e] = T(0);
+      }
+      if (in_y) {
+        gy = sd.psi_y + ((long long)k * sd.yw + ys) * px + xg;
+        ld_vec_rw(gy + PSI_S0 * sd.psy, py0);
+        ld_vec_rw(gy + PSI_S1 * sd.psy, py1);
+        ld_vec_rw(gy + PSI_S2 * sd.psy, py2);
+      } else {
+#pragma unroll
+        for (int e = 0; e < V; ++e) py0[e] = py1[e] = py2[e] = T(0);
+      }
+      if (in_z) {
+        gz = sd.psi_z + ((long long)zs * ny + y) * px + xg;
+        ld_vec_rw(gz + PSI_S0 * sd.psz, pz0);
+        ld_vec_rw(gz + PSI_S1 * sd.psz, pz1);
+        ld_vec_rw(gz + PSI_S2 * sd.psz, pz2);
+      } else {
+#pragma unroll
+        for (int e = 0; e < V; ++e) pz0[e] = pz1[e] = pz2[e] = T(0);
+      }
+
+      const bool yN = (y >= 1) && (k >= 1);   // normal stresses: j >= 2, k >= 2 (1-based)
+      const bool yXY = (y <= ny - 2);         // sigma_xy and sigma_yz: j <= NY-1
+#pragma unroll
+      for (int e = 0; e < V; ++e) {
+        const int x = xg + e;
+        const T vx_xp = (e < V - 1) ? vx_c[e + 1] : vx_e;
+        const T vy_xm = (e > 0) ? vy_c[e - 1] : vy_w;
+        const T vz_xm = (e > 0) ? vz_c[e - 1] : vz_w;
+        const T cs_xm = (e > 0) ? cs_c[e - 1] : cs_w;
+        const T rho_xm = (e > 0) ? rho_c[e - 1] : rho_w;
+
+        // normal stresses, simpelmodel.cpp:378-413
+        {
+          const bool m = yN && (x <= nx - 2);
+          const T vp = cp_c[e], vs = cs_c[e], rhos = rho_c[e];
+          const T lambda = rhos * (vp * vp - T(2) * vs * vs);
+          const T l2m = rhos * vp * vp;
+          const T DT_l2m = dt * l2m, DT_l = dt * lambda;
+          T dvx_dx = (vx_xp - vx_c[e]) * idx;
+          T dvy_dy = (vy_c[e] - vy_ym[e]) * idy;
+          T dvz_dz = (vz_c[e] - vz_zm[e]) * idz;
+          const T qx = bxh[e] * px0[e] + axh[e] * dvx_dx;
+          const T qy = by * py0[e] + ay * dvy_dy;
+          const T qz = bz * pz0[e] + az * dvz_dz;
+          dvx_dx = dvx_dx * ikxh[e] + qx;
+          dvy_dy = dvy_dy * iky + qy;
+          dvz_dz = dvz_dz * ikz + qz;
+          if (m) {
+            px0[e] = qx; py0[e] = qy; pz0[e] = qz;
+            sxx[e] = DT_l2m * dvx_dx + DT_l * (dvy_dy + dvz_dz) + sxx[e];
+            syy[e] = DT_l * (dvx_dx + dvz_dz) + DT_l2m * dvy_dy + syy[e];
+            szz[e] = DT_l * (dvx_dx + dvy_dy) + DT_l2m * dvz_dz + szz[e];
+          }
+        }
+        // sigma_xy, :416-442
+        {
+          const bool m = yXY && (x >= 1) && (x <= nx - 1);
+          const T vs = (cs_xm + cs_yp[e]) / T(2);
+          const T rhos = (rho_xm + rho_yp[e]) / T(2);
+          const T DT_mu = dt * (rhos * vs * vs);
+          T dvy_dx = (vy_c[e] - vy_xm) * idx;
+          T dvx_dy = (vx_yp[e] - vx_c[e]) * idy;
+          const T qx = bx[e] * px1[e] + ax[e] * dvy_dx;
+          const T qy = byh * py1[e] + ayh * dvx_dy;
+          dvy_dx = dvy_dx * ikx[e] + qx;
+          dvx_dy = dvx_dy * ikyh + qy;
+          if (m) {
+            px1[e] = qx; py1[e] = qy;
+            sxy[e] = DT_mu * (dvy_dx + dvx_dy) + sxy[e];
+          }
+        }
+        // sigma_xz, :445-471 (z+1 of plane nz-1 is the zero plane)
+        {
+          const bool m = (x >= 1) && (x <= nx - 1);
+          const T vs = (cs_xm + cs_zp[e]) / T(2);
+          const T rhos = (rho_xm + rho_zp[e]) / T(2);
+          const T DT_mu = dt * (rhos * vs * vs);
+          T dvz_dx = (vz_c[e] - vz_xm) * idx;
+          T dvx_dz = (vx_zp[e] - vx_c[e]) * idz;
+          const T qx = bx[e] * px2[e] + ax[e] * dvz_dx;
+          const T qz = bzh * pz1[e] + azh * dvx_dz;
+          dvz_dx = dvz_dx * ikx[e] + qx;
+          dvx_dz = dvx_dz * ikzh + qz;
+          if (m) {
+            px2[e] = qx; pz1[e] = qz;
+            sxz[e] = DT_mu * (dvz_dx + dvx_dz) + sxz[e];
+          }
+        }
+        // sigma_yz, :473-498
+        {
+          const bool m = yXY && (x <= nx - 1);
+          const T vs = (cs_yp[e] + cs_zp[e]) / T(2);
+          const T rhos = (rho_yp[e] + rho_zp[e]) / T(2);
+          const T DT_mu = dt * (rhos * vs * vs);
+          T dvz_dy = (vz_yp[e] - vz_c[e]) * idy;
+          T dvy_dz = (vy_zp[e] - vy_c[e]) * idz;
+          const T qy = byh * py2[e] + ayh * dvz_dy;
+          const T qz = bzh * pz2[e] + azh * dvy_dz;
+          dvz_dy = dvz_dy * ikyh + qy;
+          dvy_dz = dvy_dz * ikzh + qz;
+          if (m) {
+            py2[e] = qy; pz2[e] = qz;
+            syz[e] = DT_mu * (dvz_dy + dvy_dz) + syz[e];
+          }
+        }
+        vz_zm[e] = vz_c[e];
+      }
+
+      if (live) {
+        const long long g = (long long)k * plane + (long long)y * px + xg;
+        st_vec(sd.f[3] + g, sxx);
+        st_vec(sd.f[4] + g, syy);
+        st_vec(sd.f[5] + g, szz);
+        st_vec(sd.f[6] + g, sxy);
+        st_vec(sd.f[7] + g, sxz);
+        st_vec(sd.f[8] + g, syz);
+        if (in_x) {
+          st_vec(gx + PSI_S0 * sd.psx, px0);
+          st_vec(gx + PSI_S1 * sd.psx, px1);
+          st_vec(gx + PSI_S2 * sd.psx, px2);
+        }
+        if (in_y) {
+          st_vec(gy + PSI_S0 * sd.psy, py0);
+          st_vec(gy + PSI_S1 * sd.psy, py1);
+          st_vec(gy + PSI_S2 * sd.psy, py2);
+        }
+        if (in_z) {
+          st_vec(gz + PSI_S0 * sd.psz, pz0);
+          st_vec(gz + PSI_S1 * sd.psz, pz1);
+          st_vec(gz + PSI_S2 * sd.psz, pz2);
+        }
+      }
+
+      // every thread is done with stage n (and n+1 at the end of the run)
+      if (__syncthreads_or(timed_out)) {
+        if (tid == 0) atomicOr(err, DEV_ERR_TIMEOUT);
+        // let the loads already issued land before the block exits
+        for (long long q = consumed; q < pc.n; ++q)
+          mbar_wait_bounded(&full[q % NS], (uint32_t)((q / NS) & 1), 100000000ull);
+        return;
+      }
+      consumed += (k == item.k1 - 1) ? 2 : 1;
+      while (pc.item < pc.end && pc.n < consumed + NS) issue(tid == 0);
+    }
+  }
+}
+
+// --------------------------------------------------------- velocity ----
+template <typename T, int TX, int TY, int NS>
+__global__ void __launch_bounds__(Geo<T, TX, TY, NS>::NT)
+    velocity_kernel(const ShotDesc<T> *__restrict__ shots, const ShotMaps *__restrict__ maps,
+                    const Item *__restrict__ items, const int2 *__restrict__ ranges, int tick,
+                    unsigned *__restrict__ err) {
+  using G = Geo<T, TX, TY, NS>;
+  constexpr int V = G::VEC, H = G::H, WW = G::WW;
+  extern __shared__ __align__(1024) unsigned char smem[];
+  uint64_t *full = reinterpret_cast<uint64_t *>(smem + NS * G::V_STAGE);
+
+  const int tid = threadIdx.x;
+  const int tx = tid % G::NTX, ty = tid / G::NTX;
+  const int2 range = ranges[blockIdx.x];
+  if (range.x >= range.y) return;
+
+  if (tid == 0) {
+    for (int s = 0; s < NS; ++s) mbar_init(&full[s], 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+
+  LoadCursor pc{range.x, items[range.x].k0, range.y, 0};
+  auto issue = [&](bool do_copy) {
+    const Item it = items[pc.item];
+    const int txs = tiles_x_of(shots[it.shot], TX);
+    const int x0 = (it.tile % txs) * TX, y0 = (it.tile / txs) * TY;
+    const int slot = (int)(pc.n % NS);
+    if (do_copy) {
+      unsigned char *st = smem + slot * G::V_STAGE;
+      const CUtensorMap *m = maps[it.shot].vel;
+      uint64_t *bar = &full[slot];
+      mbar_arrive_expect_tx(bar, G::V_TX);
+      tma_load_3d(st + G::V_SXX, &m[0], x0 - H, y0, pc.k, bar);
+      tma_load_3d(st + G::V_SYY, &m[1], x0, y0, pc.k, bar);
+      tma_load_3d(st + G::V_SZZ, &m[2], x0, y0, pc.k, bar);
+      tma_load_3d(st + G::V_SXY, &m[3], x0, y0 - 1, pc.k, bar);
+      tma_load_3d(st + G::V_SXZ, &m[4], x0, y0, pc.k, bar);
+      tma_load_3d(st + G::V_SYZ, &m[5], x0, y0 - 1, pc.k, bar);
+      tma_load_3d(st + G::V_RHO, &m[6], x0 - H, y0, pc.k, bar);
+#pragma unroll
+      for (int c = 0; c < 3; ++c)
+        tma_load_3d(st + G::V_V + c * G::SC, &m[7 + c], x0, y0, pc.k, bar);
+    }
+    ++pc.n;
+    if (++pc.k > it.k1) {
+      if (++pc.item < pc.end) pc.k = items[pc.item].k0;
+    }
+  };
+  for (int s = 0; s < NS && pc.item < pc.end; ++s) issue(tid == 0);
+
+  long long consumed = 0;
+  bool timed_out = false;
+  constexpr int CS = G::SC / (int)sizeof(T);
+
+  for (int ii = range.x; ii < range.y; ++ii) {
+    const Item item = items[ii];
+    const ShotDesc<T> &sd = shots[item.shot];
+    const int nx = sd.nx, ny = sd.ny, nz = sd.nz, px = sd.px;
+    const int txs = tiles_x_of(sd, TX);
+    const int x0 = (item.tile % txs) * TX, y0 = (item.tile / txs) * TY;
+    const int xg = x0 + tx * V, y = y0 + ty;
+    const bool live = (xg < nx) && (y < ny);
+    const T dt = sd.dt, idx = sd.idx, idy = sd.idy, idz = sd.idz;
+    const long long plane = (long long)ny * px;
+    const int it_step = tick - sd.tick0;
+    const bool sample = (it_step % sd.sampgat == 0) && (it_step / sd.sampgat <= sd.nsamp) && it_step > 0;
+    const int samp = it_step / sd.sampgat - 1;
+
+    T sxz_zm[V], syz_zm[V];
+#pragma unroll
+    for (int e = 0; e < V; ++e) sxz_zm[e] = syz_zm[e] = T(0);
+    if (live && item.k0 > 0) {
+      const long long g = (long long)(item.k0 - 1) * plane + (long long)y * px + xg;
+      ld_vec_rw(sd.f[7] + g, sxz_zm);
+      ld_vec_rw(sd.f[8] + g, syz_zm);
+    }
+
+    const bool in_x = live && (xg < sd.xl || xg >= sd.xr);
+    const int xs = xg < sd.xl ? xg : sd.xl + (xg - sd.xr);
+    T ax[V], bx[V], ikx[V], axh[V], bxh[V], ikxh[V];
+    if (in_x) {
+      ld_vec_global(sd.prof_x + PR_A * px + xg, ax);
+      ld_vec_global(sd.prof_x + PR_B * px + xg, bx);
+      ld_vec_global(sd.prof_x + PR_IK * px + xg, ikx);
+      ld_vec_global(sd.prof_x + PR_AH * px + xg, axh);
+      ld_vec_global(sd.prof_x + PR_BH * px + xg, bxh);
+      ld_vec_global(sd.prof_x + PR_IKH * px + xg, ikxh);
+    } else {
+#pragma unroll
+      for (int e = 0; e < V; ++e) { ax[e] = axh[e] = T(0); bx[e] = bxh[e] = ikx[e] = ikxh[e] = T(1); }
+    }
+    const bool in_y = live && (y < sd.yl || y >= sd.yr);
+    const int ys = y < sd.yl ? y : sd.yl + (y - sd.yr);
+    T ay = 0, by = 1, iky = 1, ayh = 0, byh = 1, ikyh = 1;
+    if (in_y) {
+      ay = sd.prof_y[PR_A * ny + y]; by = sd.prof_y[PR_B * ny + y]; iky = sd.prof_y[PR_IK * ny + y];
+      ayh = sd.prof_y[PR_AH * ny + y]; byh = sd.prof_y[PR_BH * ny + y]; ikyh = sd.prof_y[PR_IKH * ny + y];
+    }
+    const int sl0 = ty * WW + H + tx * V;     // sxx box (origin x0-H, y0)
+    const int sr0 = ty * WW + tx * V;         // sxz box (origin x0, y0)
+    const int sr1 = (ty + 1) * WW + tx * V;   // sxy box (origin x0, y0-1): own row ty+1
+    const int sc = ty * TX + tx * V;          // syy box (origin x0, y0) / centre boxes
+    const int sc1 = (ty + 1) * TX + tx * V;   // syz box (origin x0, y0-1)
+
+    for (int k = item.k0; k < item.k1; ++k) {
+      const long long n = consumed;
+      const int s0 = (int)(n % NS), s1 = (int)((n + 1) % NS);
+      bool ok = mbar_wait_bounded(&full[s0], (uint32_t)((n / NS) & 1));
+      ok = ok && mbar_wait_bounded(&full[s1], (uint32_t)(((n + 1) / NS) & 1));
+      timed_out |= !ok;
+      const unsigned char *cur = smem + s0 * G::V_STAGE;
+      const unsigned char *nxt = smem + s1 * G::V_STAGE;
+      const T *bsxx = reinterpret_cast<const T *>(cur + G::V_SXX);
+      const T *bsyy = reinterpret_cast<const T *>(cur + G::V_SYY);
+      const T *bszz = reinterpret_cast<const T *>(cur + G::V_SZZ);
+      const T *bsxy = reinterpret_cast<const T *>(cur + G::V_SXY);
+      const T *bsxz = reinterpret_cast<const T *>(cur + G::V_SXZ);
+      const T *bsyz = reinterpret_cast<const T *>(cur + G::V_SYZ);
+      const T *brho = reinterpret_cast<const T *>(cur + G::V_RHO);
+      const T *bv = reinterpret_cast<const T *>(cur + G::V_V);
+
+      T sxx_c[V], syy_c[V], syy_yp[V], szz_c[V], szz_zp[V], sxy_c[V], sxy_ym[V], sxz_c[V];
+      T syz_c[V], syz_ym[V], rho_c[V], rho_yp[V], rho_zp[V], vx[V], vy[V], vz[V];
+      ld_vec(bsxx + sl0, sxx_c);
+      const T sxx_w = bsxx[sl0 - 1];
+      ld_vec(bsyy + sc, syy_c);
+      ld_vec(bsyy + sc + TX, syy_yp);
+      ld_vec(bszz + sc, szz_c);
+      ld_vec(reinterpret_cast<const T *>(nxt + G::V_SZZ) + sc, szz_zp);
+      ld_vec(bsxy + sr1, sxy_c);
+      ld_vec(bsxy + sr1 - WW, sxy_ym);
+      const T sxy_e = bsxy[sr1 + V];
+      ld_vec(bsxz + sr0, sxz_c);
+      const T sxz_e = bsxz[sr0 + V];
+      ld_vec(bsyz + sc1, syz_c);
+      ld_vec(bsyz + sc1 - TX, syz_ym);
+      ld_vec(brho + sl0, rho_c);
+      ld_vec(brho + sl0 + WW, rho_yp);
+      const T rho_w = brho[sl0 - 1];
+      ld_vec(reinterpret_cast<const T *>(nxt + G::V_RHO) + sl0, rho_zp);
+      ld_vec(bv + 0 * CS + sc, vx);
+      ld_vec(bv + 1 * CS + sc, vy);
+      ld_vec(bv + 2 * CS + sc, vz);
+
+      const bool in_z = live && (k < sd.zl || k >= sd.zr);
+      const int zs = k < sd.zl ? k : sd.zl + (k - sd.zr);
+      T az = 0, bz = 1, ikz = 1, azh = 0, bzh = 1, ikzh = 1;
+      if (in_z) {
+        az = sd.prof_z[PR_A * nz + k]; bz = sd.prof_z[PR_B * nz + k]; ikz = sd.prof_z[PR_IK * nz + k];
+        azh = sd.prof_z[PR_AH * nz + k]; bzh = sd.prof_z[PR_BH * nz + k]; ikzh = sd.prof_z[PR_IKH * nz + k];
+      }
+      T px0[V], px1[V], px2[V], py0[V], py1[V], py2[V], pz0[V], pz1[V], pz2[V];
+      T *gx = nullptr, *gy = nullptr, *gz = nullptr;
+      if (in_x) {
+        gx = sd.psi_x + ((long long)k * ny + y) * sd.xw + xs;
+        ld_vec_rw(gx + PSI_V0 * sd.psx, px0);
+        ld_vec_rw(gx + PSI_V1 * sd.psx, px1);
+        ld_vec_rw(gx + PSI_V2 * sd.psx, px2);
+      } else {
+#pragma unroll
+        for (int e = 0; e < V; ++e) px0[e] = px1[e] = px2[e] = T(0);
+      }
+      if (in_y) {
+        gy = sd.psi_y + ((long long)k * sd.yw + ys) * px + xg;
+        ld_vec_rw(gy + PSI_V0 * sd.psy, py0);
+        ld_vec_rw(gy + PSI_V1 * sd.psy, py1);
+        ld_vec_rw(gy + PSI_V2 * sd.psy, py2);
+      } else {
+#pragma unroll
+        for (int e = 0; e < V; ++e) py0[e] = py1[e] = py2[e] = T(0);
+      }
+      if (in_z) {
+        gz = sd.psi_z + ((long long)zs * ny + y) * px + xg;
+        ld_vec_rw(gz + PSI_V0 * sd.psz, pz0);
+        ld_vec_rw(gz + PSI_V1 * sd.psz, pz1);
+        ld_vec_rw(gz + PSI_V2 * sd.psz, pz2);
+      } else {
+#pragma unroll
+        for (int e = 0; e < V; ++e) pz0[e] = pz1[e] = pz2[e] = T(0);
+      }
+
+      const bool mvx_yz = (y >= 1) && (k >= 1);
+      const bool mvy_yz = (y <= ny - 2) && (k >= 1);
+      const bool mvz_yz = (y >= 1) && (k <= nz - 2);
+      T rbx[V], rby[V], rbz[V];   // averaged densities (reused by the source)
+#pragma unroll
+      for (int e = 0; e < V; ++e) {
+        const int x = xg + e;
+        const T sxx_xm = (e > 0) ? sxx_c[e - 1] : sxx_w;
+        const T rho_xm = (e > 0) ? rho_c[e - 1] : rho_w;
+        const T sxy_xp = (e < V - 1) ? sxy_c[e + 1] : sxy_e;
+        const T sxz_xp = (e < V - 1) ? sxz_c[e + 1] : sxz_e;
+        // vx, simpelmodel.cpp:502-530
+        {
+          const bool m = mvx_yz && (x >= 1) && (x <= nx - 1);
+          const T rhos = (rho_c[e] + rho_xm) / T(2);
+          rbx[e] = rhos;
+          const T DT_over_rho = dt / rhos;
+          T d1 = (sxx_c[e] - sxx_xm) * idx;
+          T d2 = (sxy_c[e] - sxy_ym[e]) * idy;
+          T d3 = (sxz_c[e] - sxz_zm[e]) * idz;
+          const T qx = bx[e] * px0[e] + ax[e] * d1;
+          const T qy = by * py0[e] + ay * d2;
+          const T qz = bz * pz0[e] + az * d3;
+          d1 = d1 * ikx[e] + qx;
+          d2 = d2 * iky + qy;
+          d3 = d3 * ikz + qz;
+          if (m) {
+            px0[e] = qx; py0[e] = qy; pz0[e] = qz;
+            vx[e] = DT_over_rho * (d1 + d2 + d3) + vx[e];
+          }
+        }
+        // vy, :532-559
+        {
+          const bool m = mvy_yz && (x <= nx - 2);
+          const T rhos = (rho_c[e] + rho_yp[e]) / T(2);
+          rby[e] = rhos;
+          const T DT_over_rho = dt / rhos;
+          T d1 = (sxy_xp - sxy_c[e]) * idx;
+          T d2 = (syy_yp[e] - syy_c[e]) * idy;
+          T d3 = (syz_c[e] - syz_zm[e]) * idz;
+          const T qx = bxh[e] * px1[e] + axh[e] * d1;
+          const T qy = byh * py1[e] + ayh * d2;
+          const T qz = bz * pz1[e] + az * d3;
+          d1 = d1 * ikxh[e] + qx;
+          d2 = d2 * ikyh + qy;
+          d3 = d3 * ikz + qz;
+          if (m) {
+            px1[e] = qx; py1[e] = qy; pz1[e] = qz;
+            vy[e] = DT_over_rho * (d1 + d2 + d3) + vy[e];
+          }
+        }
+        // vz, :563-590
+        {
+          const bool m = mvz_yz && (x <= nx - 2);
+          const T rhos = (rho_c[e] + rho_zp[e]) / T(2);
+          rbz[e] = rhos;
+          const T DT_over_rho = dt / rhos;
+          T d1 = (sxz_xp - sxz_c[e]) * idx;
+          T d2 = (syz_c[e] - syz_ym[e]) * idy;
+          T d3 = (szz_zp[e] - szz_c[e]) * idz;
+          const T qx = bxh[e] * px2[e] + axh[e] * d1;
+          const T qy = by * py2[e] + ay * d2;
+          const T qz = bzh * pz2[e] + azh * d3;
+          d1 = d1 * ikxh[e] + qx;
+          d2 = d2 * iky + qy;
+          d3 = d3 * ikzh + qz;
+          if (m) {
+            px2[e] = qx; py2[e] = qy; pz2[e] = qz;
+            vz[e] = DT_over_rho * (d1 + d2 + d3) + vz[e];
+          }
+        }
+        sxz_zm[e] = sxz_c[e];
+        syz_zm[e] = syz_c[e];
+      }
+
+      if (live) {
+        // receivers in this row segment (velocity after the update, :593-602)
+        if (sample) {
+          int lo = sd.rec_plane[k], hi = sd.rec_plane[k + 1];
+          if (lo < hi) {
+            while (lo < hi) {   // first receiver with (j, i) >= (y, xg)
+              const int mid = (lo + hi) >> 1;
+              const int4 r = sd.rec_sorted[mid];
+              if (r.y < y || (r.y == y && r.x < xg)) lo = mid + 1; else hi = mid;
+            }
+            for (int q = lo, qe = sd.rec_plane[k + 1]; q < qe; ++q) {
+              const int4 r = sd.rec_sorted[q];
+              if (r.y != y || r.x >= xg + V) break;
+              const int e = r.x - xg;
+              T rvx = vx[0], rvy = vy[0], rvz = vz[0];
+#pragma unroll
+              for (int c = 1; c < V; ++c) {
+                rvx = (c == e) ? vx[c] : rvx;
+                rvy = (c == e) ? vy[c] : rvy;
+                rvz = (c == e) ? vz[c] : rvz;
+              }
+              T *out = sd.seis + (long long)r.w * 3 * sd.nsamp + samp;
+              out[0] = rvx;
+              out[sd.nsamp] = rvy;
+              out[2 * sd.nsamp] = rvz;
+            }
+          }
+        }
+        // force source after the update (cudazerocopy.cu:451-453)
+        if (sd.src_kind == 0 && k == sd.src_k && y == sd.src_j && sd.src_i >= xg && sd.src_i < xg + V &&
+            it_step >= 1 && it_step <= sd.nstep) {
+          const T s = sd.stf[it_step - 1];
+          const int se = sd.src_i - xg;
+          const bool wx = sd.src_w[0] != T(0), wy = sd.src_w[1] != T(0), wz = sd.src_w[2] != T(0);
+          const T fx = sd.src_w[0] * s, fy = sd.src_w[1] * s, fz = sd.src_w[2] * s;
+#pragma unroll
+          for (int c = 0; c < V; ++c) {
+            const bool hit = (c == se);
+            vx[c] = (hit && wx) ? vx[c] + fx * dt / rbx[c] : vx[c];
+            vy[c] = (hit && wy) ? vy[c] + fy * dt / rby[c] : vy[c];
+            vz[c] = (hit && wz) ? vz[c] + fz * dt / rbz[c] : vz[c];
+          }
+        }
+        const long long g = (long long)k * plane + (long long)y * px + xg;
+        st_vec(sd.f[0] + g, vx);
+        st_vec(sd.f[1] + g, vy);
+        st_vec(sd.f[2] + g, vz);
+        if (in_x) {
+          st_vec(gx + PSI_V0 * sd.psx, px0);
+          st_vec(gx + PSI_V1 * sd.psx, px1);
+          st_vec(gx + PSI_V2 * sd.psx, px2);
+        }
+        if (in_y) {
+          st_vec(gy + PSI_V0 * sd.psy, py0);
+          st_vec(gy + PSI_V1 * sd.psy, py1);
+          st_vec(gy + PSI_V2 * sd.psy, py2);
+        }
+        if (in_z) {
+          st_vec(gz + PSI_V0 * sd.psz, pz0);
+          st_vec(gz + PSI_V1 * sd.psz, pz1);
+          st_vec(gz + PSI_V2 * sd.psz, pz2);
+        }
+      }
+
+      if (__syncthreads_or(timed_out)) {
+        if (tid == 0) atomicOr(err, DEV_ERR_TIMEOUT);
+        for (long long q = consumed; q < pc.n; ++q)
+          mbar_wait_bounded(&full[q % NS], (uint32_t)((q / NS) & 1), 100000000ull);
+        return;
+      }
+      consumed += (k == item.k1 - 1) ? 2 : 1;
+      while (pc.item < pc.end && pc.n < consumed + NS) issue(tid == 0);
+    }
+  }
+}
+
+}  // namespace ela3d

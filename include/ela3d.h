@@ -1,0 +1,188 @@
+/*
+ * ela3d.h -- C ABI of the GB300 SEISMIC_CPML engine (libela3d.so).
+ *
+ * The reference (thejatmik/ela3d) has no library API: the simulation call is
+ * the body of main() in seismicCPML_3d_isotropic_simpelmodel.cpp, and its
+ * parameter surface is the set of locals assigned at the top of main().  Each
+ * entry point below names the reference code it stands in for.  All sizes and
+ * indices are plain integers, all buffers plain host pointers; no CUDA or
+ * PyTorch types cross this boundary.
+ *
+ * Conventions
+ *  - Every call returns ela3d_status (0 = OK) and never exits the process
+ *    (the reference's HANDLE_ERROR calls exit(), seismicCPML_3d_isotropic_cudazerocopy.cu:142-151).
+ *  - Grid indices are 0-based.  Cell (i, j, k) is the reference's 1-based
+ *    cell (i+1, j+1, k+1); x is the fastest axis, k grows downwards (depth).
+ *  - Host model and output arrays are compact nx*ny*nz, x fastest, the layout
+ *    of the reference's model*.bin and v*%05i.bin files.
+ *  - A plan owns its device memory and one CUDA stream.  Use one plan from
+ *    one thread at a time.  A server object is internally synchronised.
+ */
+#ifndef ELA3D_H
+#define ELA3D_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ELA3D_VERSION_MAJOR 0
+#define ELA3D_VERSION_MINOR 1
+
+typedef enum ela3d_status {
+    ELA3D_OK = 0,
+    ELA3D_ERR_INVALID_ARG = 1,
+    ELA3D_ERR_OOM = 2,
+    ELA3D_ERR_CUDA = 3,
+    ELA3D_ERR_UNSTABLE = 4,   /* energy monitor saw growth or a non-finite value */
+    ELA3D_ERR_TIMEOUT = 5,    /* a device-side wait gave up (kernel returned early) */
+    ELA3D_ERR_NO_DEVICE = 6,
+    ELA3D_ERR_BUSY = 7,       /* admission refused: not enough device memory / slots */
+    ELA3D_ERR_CANCELLED = 8,
+    ELA3D_ERR_NOT_FOUND = 9,
+    ELA3D_ERR_NOT_READY = 10
+} ela3d_status;
+
+/* Arithmetic of the time loop.  FP32 is the production path; FP64 is the
+ * checking build of the same kernels. */
+enum { ELA3D_FP32 = 0, ELA3D_FP64 = 1 };
+
+/* C-PML profile variant.  COMPAT reproduces the reference CPU program's
+ * profile code as written (simpelmodel.cpp:142-361: a_x_half never set at
+ * :223, z normalised by the y thickness and the zmin half-node test reading a
+ * stale y abscissa at :326-350).  CLEAN is the textbook C-PML of the same
+ * formulas.  The time-loop kernels are identical for both. */
+enum { ELA3D_PML_COMPAT = 0, ELA3D_PML_CLEAN = 1 };
+
+/* Source time function: Ricker (elatic_3d_unified_cuda_memory.cu:441), first
+ * derivative of a Gaussian (simpelmodel.cpp:610), Gaussian (:438 commented). */
+enum { ELA3D_STF_RICKER = 0, ELA3D_STF_GAUSS_DERIV = 1, ELA3D_STF_GAUSS = 2 };
+
+/* Injection: FORCE adds w_c*s*dt/rho_c to velocity component c, rho averaged
+ * as in that component's update (cudazerocopy.cu:451-453); EXPLOSIVE adds
+ * s*dt*(lambda+2mu) into the normal stresses with the angle weights of
+ * simpelmodel.cpp:611-622. */
+enum { ELA3D_SRC_FORCE = 0, ELA3D_SRC_EXPLOSIVE = 1 };
+
+/* Field components for ela3d_get_field. */
+enum {
+    ELA3D_VX = 0, ELA3D_VY = 1, ELA3D_VZ = 2,
+    ELA3D_SXX = 3, ELA3D_SYY = 4, ELA3D_SZZ = 5,
+    ELA3D_SXY = 6, ELA3D_SXZ = 7, ELA3D_SYZ = 8
+};
+
+/* The reference's parameter surface (simpelmodel.cpp:19-78,148-153). */
+typedef struct ela3d_params {
+    int32_t nx, ny, nz;       /* NIMX, NIMY, NIMZ (cells) */
+    int32_t nstep;            /* NSTEP: length of the seismogram buffers */
+    double dx, dy, dz;        /* DELTAX/Y/Z [m] */
+    double dt;                /* DELTATT [s] */
+    int32_t npml;             /* NPOINTS_PML on all six faces */
+    int32_t pml_mode;         /* ELA3D_PML_* */
+    double npower;            /* NPOWER */
+    double k_max;             /* K_MAX_PML */
+    double alpha_max;         /* ALPHA_MAX_PML; < 0 selects pi*f0 as the reference */
+    double rcoef;             /* Rcoef */
+    double vpml;              /* vpml (the reference fixes 3000 m/s) */
+    double f0, t0, factor;    /* source frequency, delay, amplitude */
+    int32_t stf;              /* ELA3D_STF_* */
+    int32_t src_kind;         /* ELA3D_SRC_* */
+    int32_t src_i, src_j, src_k;  /* ISOURCE/JSOURCE/KSOURCE, 0-based */
+    int32_t sampgat;          /* record every sampgat steps (step % sampgat == 0) */
+    double src_w[3];          /* FORCE weights for vx, vy, vz */
+    double angle_force;       /* ANGLE_FORCE [deg] for EXPLOSIVE */
+    const int32_t *rec;       /* nrec receiver cells (i, j, k), 0-based */
+    int32_t nrec;
+    int32_t precision;        /* ELA3D_FP32 / ELA3D_FP64 */
+    int32_t it_output;        /* snapshot cadence for ela3d_set_output (0 = none) */
+    int32_t energy_every;     /* stability check cadence in steps (0 = off) */
+} ela3d_params;
+
+typedef struct ela3d_plan ela3d_plan;
+
+typedef struct ela3d_plan_info {
+    int32_t nx, ny, nz, pitch_x;   /* device row pitch in elements */
+    int32_t step;                  /* steps completed */
+    int32_t nsamp;                 /* samples per seismogram trace */
+    int32_t nrec;
+    int32_t precision;
+    int64_t device_bytes;          /* device memory owned by the plan */
+    int32_t slab_lo[3], slab_hi[3]; /* C-PML slab: cells [0,lo) and [hi,n) per axis */
+} ela3d_plan_info;
+
+/* ---- library ---------------------------------------------------------- */
+const char *ela3d_version(void);
+const char *ela3d_status_string(ela3d_status s);
+/* Message of the last failed call on this thread (empty if none). */
+const char *ela3d_last_error(void);
+
+/* Fills p with the reference CPU program's defaults (simpelmodel.cpp:19-78):
+ * 500^3 cells, dx=10, dt=1e-3, NSTEP=1000, npml=10, NPOWER=2, K_MAX=1,
+ * alpha_max=pi*f0, Rcoef=1e-3, vpml=3000, f0=35, t0=1.2/f0, factor=1e7,
+ * Gaussian-derivative explosive source at (DIMX/2, DIMY/2, 11) in 1-based
+ * cells, sampgat=2, IT_OUTPUT=200, COMPAT profiles, FP32. */
+ela3d_status ela3d_params_default(ela3d_params *p);
+
+/* ---- single shot -------------------------------------------------------- */
+/* Replaces main()'s setup: allocations and zero fill (simpelmodel.cpp:80-140),
+ * model fill (:41-59), profile precompute (:142-361).  cp, cs, rho are host
+ * arrays of nx*ny*nz float32, copied; the caller keeps ownership. */
+ela3d_status ela3d_plan_create(const ela3d_params *p, const float *cp, const float *cs,
+                               const float *rho, ela3d_plan **out);
+/* Advances nsteps time steps (the it loop, simpelmodel.cpp:376-726) and
+ * waits for completion; resumable.  Returns ELA3D_ERR_UNSTABLE when the
+ * energy monitor trips, ELA3D_ERR_TIMEOUT when a kernel gave up a wait. */
+ela3d_status ela3d_run(ela3d_plan *plan, int32_t nsteps);
+/* Queues nsteps on the plan's stream without waiting. */
+ela3d_status ela3d_enqueue(ela3d_plan *plan, int32_t nsteps);
+/* Waits for queued work and reports device-side errors. */
+ela3d_status ela3d_sync(ela3d_plan *plan);
+/* Seismograms [nrec][3][nsamp] (vx, vy, vz), nsamp = nstep / sampgat: the
+ * receiver gather of simpelmodel.cpp:593-602 sampled as at :625. */
+ela3d_status ela3d_get_seismograms(ela3d_plan *plan, float *out);
+ela3d_status ela3d_get_seismograms_f64(ela3d_plan *plan, double *out);
+/* Current field, compact nx*ny*nz (snapshot of simpelmodel.cpp:685-722). */
+ela3d_status ela3d_get_field(ela3d_plan *plan, int32_t comp, float *out);
+ela3d_status ela3d_get_field_f64(ela3d_plan *plan, int32_t comp, double *out);
+/* Total kinetic + strain energy [J], FP64 device reduction (no counterpart
+ * in the reference; the stability monitor). */
+ela3d_status ela3d_energy(ela3d_plan *plan, double *out);
+ela3d_status ela3d_plan_info_get(ela3d_plan *plan, ela3d_plan_info *out);
+/* Per-kernel CUDA-event timing of subsequent launches (0 = off). */
+ela3d_status ela3d_set_kernel_timing(ela3d_plan *plan, int32_t enable);
+/* Sums since timing was enabled: stress and velocity kernel milliseconds
+ * and launch counts. */
+ela3d_status ela3d_get_kernel_timing(ela3d_plan *plan, double *stress_ms, double *velocity_ms,
+                                     int64_t *stress_launches, int64_t *velocity_launches);
+ela3d_status ela3d_plan_destroy(ela3d_plan *plan);
+
+/* ---- kernel variants and tuning ----------------------------------------- */
+/* A compiled instance of the stress/velocity kernel pair: real type, x-y
+ * tile and shared-memory pipeline depth.  No counterpart in the reference
+ * (its kernels use fixed 10^3 thread blocks, cudazerocopy.cu:1361-1369). */
+typedef struct ela3d_variant_info {
+    int32_t fp64, tile_x, tile_y, stages, threads;
+    int32_t stress_smem, velocity_smem;
+} ela3d_variant_info;
+
+/* Work schedule: kind 0 = equal contiguous share of (tile, plane) units per
+ * block; kind 1 = z-chunks of `chunk` planes dealt round-robin.  Negative
+ * fields select the built-in default. */
+typedef struct ela3d_tuning {
+    int32_t variant;        /* index < ela3d_variant_count(), or -1 */
+    int32_t schedule;       /* 0, 1, or -1 */
+    int32_t chunk;          /* planes per z-chunk for schedule 1 */
+    int32_t blocks_per_sm;  /* cap on resident blocks per SM, 0 = occupancy limit */
+} ela3d_tuning;
+
+int32_t ela3d_variant_count(void);
+ela3d_status ela3d_variant_get(int32_t index, ela3d_variant_info *out);
+/* ela3d_plan_create with an explicit kernel variant and schedule. */
+ela3d_status ela3d_plan_create_tuned(const ela3d_params *p, const float *cp, const float *cs,
+                                     const float *rho, const ela3d_tuning *tune, ela3d_plan **out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

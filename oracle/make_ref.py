@@ -1,0 +1,188 @@
+"""Build the reference CPU program as a parity oracle.  TEST INFRASTRUCTURE.
+
+Reads the unmodified reference source
+``seismicCPML_3d_isotropic_simpelmodel.cpp`` from the reference checkout,
+applies a mechanical parameter patch, and writes the result plus binaries
+into ``oracle/_ref/`` (git-ignored; nothing from the reference is committed).
+
+The patch only turns hard-coded literals into fields of ``g_cfg``
+(oracle/ref_harness.h) and adds hooks; the time-loop arithmetic is left as
+written.  Changes, each asserted to match exactly the expected number of
+times so that a different reference fails loudly:
+
+- main() reads a config file; NIMX/NIMY/NIMZ, NSTEP, DELTATT, sampgat,
+  IT_OUTPUT, DELTAX, f0, t0, factor, NPOINTS_PML, source position, angle,
+  NPOWER, K_MAX_PML, ALPHA_MAX_PML, Rcoef and vpml come from it (:20-153);
+- every full-grid malloc becomes a calloc with one extra z-plane, so the
+  read of plane NIMZ+1 by the sigma_xz/sigma_yz loop (:450,:477) sees zeros;
+- the model is loaded from binary files after the constant fill (:45-59);
+- the source time function may be the Ricker (elatic_3d_unified_cuda_memory.cu:441)
+  and the injection a force into velocity
+  (seismicCPML_3d_isotropic_cudazerocopy.cu:451-453), selected by config;
+- per-step console output is removed;
+- receivers are recorded from the velocity after the update, before the
+  source, exactly where the program gathers its plane (:592-604);
+- optional "clean" switch fixes the a_x_half assignment (:223) and the zmin
+  half-node abscissa (:331) and per-axis z normalisation, for checking the
+  textbook C-PML variant;
+- a float64 variant replaces ``float`` by ``double`` and the f-suffixed
+  libm calls by their double versions.
+
+Usage: python oracle/make_ref.py [--ref DIR] [--no-build]
+"""
+from __future__ import annotations
+
+import argparse
+import os
+import re
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+OUT = os.path.join(HERE, "_ref")
+REF_NAME = "seismicCPML_3d_isotropic_simpelmodel.cpp"
+DEFAULT_REF_DIR = "/root/reference"
+
+
+def _sub(src: str, old: str, new: str, count: int = 1) -> str:
+    n = src.count(old)
+    if n != count:
+        raise RuntimeError(f"patch anchor matched {n} times (expected {count}): {old!r}")
+    return src.replace(old, new)
+
+
+def patch(src: str) -> str:
+    s = src.replace("\r\n", "\n")
+    s = _sub(s, '#include "conio.h"', '#include "conio.h"\n#include "ref_harness.h"')
+    s = _sub(s, "int main(void) {", "int main(int argc, char **argv) {\n\tref_load_cfg(argc, argv);")
+    for name, field in (("NIMX = 500;", "NIMX = g_cfg.nx;"), ("NIMY = 500;", "NIMY = g_cfg.ny;"),
+                        ("NIMZ = 500;", "NIMZ = g_cfg.nz;")):
+        s = _sub(s, name, field)
+    s = _sub(s, "int Ngatx = 100;", "int Ngatx = g_cfg.ngatx;")
+    s = _sub(s, "int Ngaty = 5;", "int Ngaty = g_cfg.ngaty;")
+    s = _sub(s, "int NSTEP = 1000;", "int NSTEP = g_cfg.nstep;")
+    s = _sub(s, "float DELTATT = 1e-3;", "float DELTATT = g_cfg.dt;")
+    s = _sub(s, "int sampgat = 2;", "int sampgat = g_cfg.sampgat;")
+    s = _sub(s, "int IT_OUTPUT = 200;", "int IT_OUTPUT = g_cfg.it_output;")
+    s = _sub(s, "DELTAX = 10;", "DELTAX = g_cfg.dx;")
+    s = _sub(s, "(float*)malloc(sizeof(float)*(DIMX*DIMY*DIMZ))",
+             "(float*)calloc(1, sizeof(float)*(DIMX*DIMY*(DIMZ+1)))", count=30)
+    s = _sub(s, "\tfloat f0, t0, factor;",
+             "\tref_load_model(ccp, ccs, crho, NIMX, NIMY, NIMZ);\n\tfloat f0, t0, factor;")
+    s = _sub(s, "f0 = 35;", "f0 = g_cfg.f0;")
+    s = _sub(s, "t0 = 1.2 / f0;", "t0 = g_cfg.t0;")
+    s = _sub(s, "factor = 1e+7;", "factor = g_cfg.factor;")
+    s = _sub(s, "int NPOINTS_PML = 10;", "int NPOINTS_PML = g_cfg.npml;")
+    s = _sub(s, "ISOURCEE = DIMX / 2;", "ISOURCEE = g_cfg.src_i + 1;")
+    s = _sub(s, "JSOURCEE = DIMY / 2;", "JSOURCEE = g_cfg.src_j + 1;")
+    s = _sub(s, "KSOURCEE = 11;", "KSOURCEE = g_cfg.src_k + 1;")
+    s = _sub(s, "float ANGLE_FORCEE = 0;", "float ANGLE_FORCEE = g_cfg.angle;")
+    s = _sub(s, "float NPOWER = 2;", "float NPOWER = g_cfg.npower;")
+    s = _sub(s, "float K_MAX_PML = 1;", "float K_MAX_PML = g_cfg.k_max;")
+    s = _sub(s, "float ALPHA_MAX_PML = 2 * PI*(f0 / 2);",
+             "float ALPHA_MAX_PML = 2 * PI*(f0 / 2);\n\tif (g_cfg.alpha_max >= 0) ALPHA_MAX_PML = g_cfg.alpha_max;")
+    s = _sub(s, "Rcoef = 0.001;", "Rcoef = g_cfg.rcoef;")
+    s = _sub(s, "float vpml = 3000;", "float vpml = g_cfg.vpml;")
+    # optional textbook fixes (off unless the config says clean 1)
+    s = _sub(s, "{ calpha_x_half[i] = cd_x_half[i] * (cb_x_half[i] - 1.0)",
+             "{ (g_cfg.clean ? ca_x_half[i] : calpha_x_half[i]) = cd_x_half[i] * (cb_x_half[i] - 1.0)")
+    head, zsec = s.split("//-----------------PML Z", 1)
+    zsec, tail = zsec.split("float *gatvx", 1)
+    zsec = _sub(zsec, "abscissa_in_PML = yoriginbottom - (yval + DELTAY / 2.0);",
+                "abscissa_in_PML = g_cfg.clean ? (zoriginbottom - (zval + DELTAZ / 2.0)) : "
+                "(yoriginbottom - (yval + DELTAY / 2.0));")
+    zsec = _sub(zsec, "abscissa_normalized = abscissa_in_PML / thickness_PML_y;",
+                "abscissa_normalized = abscissa_in_PML / (g_cfg.clean ? thickness_PML_z : thickness_PML_y);",
+                count=3)
+    s = head + "//-----------------PML Z" + zsec + "float *gatvx" + tail
+    # time loop hooks
+    s = _sub(s, "for (int it = 1; it <= NSTEP; it++) {",
+             "for (int it = 1; it <= NSTEP; it++) {\n\t\tref_step_hook(it);")
+    s = _sub(s, "}//end it", "}//end it\n\tref_step_hook(NSTEP + 1);")
+    s = _sub(s, "\t\t//addsource", "\t\tref_record(it, cvx, cvy, cvz, NIMX, NIMY);\n\t\t//addsource")
+    s = _sub(s, "cout << endl << lesource;", "")
+    s = _sub(s, "cout << endl << it;", "")
+    s = _sub(s, 'cout << endl << xlen << " " << ylen;', "")
+    s = _sub(s, "float source_term = -factor * 2.0*a*(t - t0)*expf(-a*powf((t - t0), 2));",
+             "float source_term = (g_cfg.stf == 1) ? (float)(-factor * 2.0*a*(t - t0)*expf(-a*powf((t - t0), 2)))"
+             " : (g_cfg.stf == 2) ? (float)(factor * expf(-a*powf((t - t0), 2)))"
+             " : (float)(factor*(1.0 - 2.0*a*powf((t - t0), 2))*expf(-a*powf(t - t0, 2)));")
+    s = _sub(s, "\t\tcsigmaxx[lesource] = csigmaxx[lesource] + force_x*DELTATT * lambdaplus2mu;",
+             "\t\tif (g_cfg.src_kind == 1) {\n"
+             "\t\tcsigmaxx[lesource] = csigmaxx[lesource] + force_x*DELTATT * lambdaplus2mu;")
+    s = _sub(s, "\t\tcsigmazz[lesource] = csigmazz[lesource] + force_y*DELTATT * lambdaplus2mu;",
+             "\t\tcsigmazz[lesource] = csigmazz[lesource] + force_y*DELTATT * lambdaplus2mu;\n"
+             "\t\t} else {\n"
+             "\t\tif (g_cfg.w[0] != 0.0) { float fsrc = (float)g_cfg.w[0] * source_term;"
+             " cvx[lesource] = cvx[lesource] + fsrc*DELTATT / ((crho[lesource] + crho[lesource - 1]) / 2); }\n"
+             "\t\tif (g_cfg.w[1] != 0.0) { float fsrc = (float)g_cfg.w[1] * source_term;"
+             " cvy[lesource] = cvy[lesource] + fsrc*DELTATT / ((crho[lesource] + crho[lesource + NIMX]) / 2); }\n"
+             "\t\tif (g_cfg.w[2] != 0.0) { float fsrc = (float)g_cfg.w[2] * source_term;"
+             " cvz[lesource] = cvz[lesource] + fsrc*DELTATT / ((crho[lesource] + crho[lesource + NIMX * NIMY]) / 2); }\n"
+             "\t\t}")
+    s = _sub(s, "\tfree(cvx); ",
+             "\tref_finish(cvx, cvy, cvz, csigmaxx, csigmayy, csigmazz, csigmaxy, csigmaxz, csigmayz,"
+             " NIMX, NIMY, NIMZ);\n\tfree(cvx); ")
+    return s
+
+
+def to_f64(s: str) -> str:
+    s = re.sub(r"\bfloat\b", "double", s)
+    for f in ("expf", "powf", "logf", "sinf", "cosf"):
+        s = re.sub(r"\b%s\(" % f, f[:-1] + "(", s)
+    return s
+
+
+def compiler_cmd(src: str, exe: str) -> list[str]:
+    return ["g++", "-O3", "-ffp-contract=off", "-w", "-Dsprintf_s=sprintf",
+            "-I", OUT, "-I", HERE, src, "-o", exe]
+
+
+def generate(ref_dir: str) -> None:
+    with open(os.path.join(ref_dir, REF_NAME), "r", encoding="latin-1") as f:
+        src = f.read()
+    os.makedirs(OUT, exist_ok=True)
+    p32 = patch(src)
+    with open(os.path.join(OUT, "ref_f32.cpp"), "w") as f:
+        f.write(p32)
+    with open(os.path.join(OUT, "ref_f64.cpp"), "w") as f:
+        f.write(to_f64(p32))
+    with open(os.path.join(OUT, "conio.h"), "w") as f:
+        f.write("/* empty stand-in for the Windows console header */\n")
+
+
+def build() -> list[str]:
+    """Compile whatever patched sources exist in oracle/_ref (no reference read)."""
+    built = []
+    procs = []
+    for v in ("f32", "f64"):
+        src = os.path.join(OUT, f"ref_{v}.cpp")
+        if not os.path.exists(src):
+            continue
+        exe = os.path.join(OUT, f"ref_{v}")
+        procs.append((exe, subprocess.Popen(compiler_cmd(src, exe))))
+    for exe, p in procs:
+        if p.wait() != 0:
+            raise RuntimeError(f"building {exe} failed")
+        built.append(exe)
+    return built
+
+
+def main() -> int:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--ref", default=DEFAULT_REF_DIR)
+    ap.add_argument("--no-build", action="store_true")
+    a = ap.parse_args()
+    if os.path.exists(os.path.join(a.ref, REF_NAME)):
+        generate(a.ref)
+    elif not os.path.exists(os.path.join(OUT, "ref_f32.cpp")):
+        print("reference source not found and no patched copy present", file=sys.stderr)
+        return 1
+    if not a.no_build:
+        for exe in build():
+            print(exe)
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

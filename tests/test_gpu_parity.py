@@ -1,0 +1,130 @@
+"""GPU parity: the sm_103a kernels through the C ABI against the oracle.
+
+The oracle is the C restatement of the reference CPU program
+(seismicCPML_3d_isotropic_simpelmodel.cpp), pinned bit-for-bit to that
+program in tests/test_oracle_pin.py.  Tolerances:
+  FP32 GPU vs FP32 oracle: relative L2 <= 2e-5 on every seismogram and field
+    (same formulas; the GPU fuses multiply-adds and multiplies by 1/K);
+  FP64 GPU vs FP64 oracle: relative L2 <= 1e-11;
+  kernel variants and schedules: bit-identical to each other.
+"""
+import numpy as np
+import pytest
+
+from conftest import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+TOL32 = 2e-5
+TOL64 = 1e-11
+
+
+def small_case(**kw):
+    from ela3d_gb300 import ShotParams, media
+
+    nx, ny, nz = kw.pop("shape", (40, 34, 46))
+    rec = [[x, ny // 2, nz // 2 - 3] for x in range(1, nx - 1, 5)]
+    rec += [[nx // 2, ny // 2, nz // 2], [0, 0, 0], [nx - 1, ny - 1, nz - 1], [3, ny - 2, 1]]
+    p = ShotParams(nx=nx, ny=ny, nz=nz, nstep=100, dt=1e-3, npml=6, f0=22.0, t0=1.2 / 22.0,
+                   src=(nx // 2, ny // 2, nz // 2), rec=np.array(rec, np.int32), sampgat=1)
+    p = p.with_(**kw)
+    cp, cs, rho = media.anticline_layers(nx, ny, nz, depths=(nz * 0.25, nz * 0.5, nz * 0.7, nz * 2),
+                                         amp=nz * 0.08, sigma=nx * 0.25, seed=7)
+    return p, cp, cs, rho
+
+
+def run_gpu(p, cp, cs, rho, nsteps=None, **tune):
+    from ela3d_gb300 import Plan
+
+    with Plan(p, cp, cs, rho, **tune) as plan:
+        plan.run(p.nstep if nsteps is None else nsteps)
+        fp64 = p.precision == 1
+        seis = plan.seismograms(fp64=fp64)
+        fields = np.stack([plan.field(c, fp64=fp64) for c in range(9)])
+    return seis, fields
+
+
+def check(seis, fields, want_s, want_f, tol):
+    assert rel_l2(seis, want_s) <= tol, rel_l2(seis, want_s)
+    for c in range(9):
+        assert rel_l2(fields[c], want_f[c]) <= tol, (c, rel_l2(fields[c], want_f[c]))
+
+
+CASES = {
+    "ricker_vz_compat": {},
+    "ricker_vz_clean": {"pml_mode": 1},
+    "explosive_gauss_deriv": {"stf": 1, "src_kind": 1},
+    "explosive_angle": {"stf": 1, "src_kind": 1, "angle_force": 35.0},
+    "force_xyz_gauss": {"stf": 2, "src_w": (0.7, -0.4, 1.0)},
+    "sampgat3_odd_shape": {"sampgat": 3, "shape": (37, 29, 31)},
+    "thin_z": {"shape": (52, 44, 14), "npml": 4},
+    "pml_covers_grid": {"shape": (16, 18, 20), "npml": 9, "nstep": 60},
+    "no_pml": {"npml": 0},
+}
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_fp32_matches_oracle(built, name):
+    import oracle
+
+    p, cp, cs, rho = small_case(**CASES[name])
+    seis, fields = run_gpu(p, cp, cs, rho)
+    want_s, want_f = oracle.run(p, cp, cs, rho)
+    check(seis, fields, want_s, want_f, TOL32)
+
+
+@pytest.mark.parametrize("name", ["ricker_vz_compat", "ricker_vz_clean", "explosive_gauss_deriv"])
+def test_fp64_matches_oracle(built, name):
+    import oracle
+
+    p, cp, cs, rho = small_case(**CASES[name])
+    p = p.with_(precision=1)
+    seis, fields = run_gpu(p, cp, cs, rho)
+    want_s, want_f = oracle.run(p, cp, cs, rho, fp64=True)
+    check(seis, fields, want_s, want_f, TOL64)
+
+
+def test_variants_and_schedules_bit_identical(built):
+    import ela3d_gb300
+
+    p, cp, cs, rho = small_case(nstep=40, pml_mode=1)
+    ref = None
+    for i, v in enumerate(ela3d_gb300.variants()):
+        if v.fp64:
+            continue
+        for sched, chunk in ((0, 0), (1, 5), (1, 64)):
+            seis, fields = run_gpu(p, cp, cs, rho, variant=i, schedule=sched, chunk=chunk)
+            if ref is None:
+                ref = (seis, fields)
+            else:
+                assert np.array_equal(seis, ref[0]), (i, sched, chunk)
+                assert np.array_equal(fields, ref[1]), (i, sched, chunk)
+
+
+def test_resume_equals_single_run(built):
+    from ela3d_gb300 import Plan
+
+    p, cp, cs, rho = small_case(nstep=60)
+    one_s, one_f = run_gpu(p, cp, cs, rho)
+    with Plan(p, cp, cs, rho) as plan:
+        plan.run(17)
+        plan.run(0)
+        plan.run(43)
+        assert plan.info().step == 60
+        s = plan.seismograms()
+        f = np.stack([plan.field(c) for c in range(9)])
+    assert np.array_equal(s, one_s)
+    assert np.array_equal(f, one_f)
+
+
+def test_energy_positive_and_decays(built):
+    from ela3d_gb300 import Plan
+
+    p, cp, cs, rho = small_case(nstep=400, npml=8)
+    with Plan(p, cp, cs, rho) as plan:
+        plan.run(150)
+        e1 = plan.energy()
+        plan.run(250)
+        e2 = plan.energy()
+    assert np.isfinite(e1) and e1 > 0
+    assert e2 < e1
