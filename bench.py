@@ -1,0 +1,372 @@
+"""Benchmark: Gcell-updates/s of the SEISMIC_CPML time loop on GB300.
+
+Workload (one "step" = one time step, stress + velocity half-steps, over
+every cell of one shot): the 256^3 four-layer anticline shot in FP32
+(dt 1e-3 s, 16 PML cells, Ricker 12 Hz on vz, 201-receiver line), synthetic
+model from numpy default_rng(0).  Every step streams ~2.4 GB, far more than
+the 129 MB L2, so no flush is needed between steps.
+
+Own arm (default): per rank one resident shot; W untimed warm-up steps, then
+K steps timed with CUDA events on the plan's stream between barriers, max
+over ranks.  Also reported:
+  roofline  the dominant kernel's algorithmic bytes per launch / its mean
+            CUDA-event duration, against MEASURED_PEAKS.json hbm_gbs;
+  e2e       one full 2000-step shot through the C ABI from host arrays
+            (plan creation with the model upload, the run, the seismogram
+            read-back), wall clock;
+  cpu_baseline  the reference CPU program (oracle/_ref, else the oracle's C
+            restatement) on 1 core, a bounded sample of the same shot.
+Reference arm (--impl reference): the reference CPU program itself on all
+host cores (one process per core, each a bounded sample of the same shot),
+rank 0 only.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+METRIC = "Gcell-updates/s"
+WORKLOAD = "anticline_256"
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+# ------------------------------------------------------------------ env --
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class Dist:
+    def __init__(self, world: int, use_cuda: bool):
+        self.world = world
+        self.pg = None
+        if world > 1:
+            import torch.distributed as dist
+
+            dist.init_process_group(backend="gloo")
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, v: float) -> float:
+        if not self.pg:
+            return v
+        import torch
+
+        t = torch.tensor([v], dtype=torch.float64)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, v: float) -> float:
+        if not self.pg:
+            return v
+        import torch
+
+        t = torch.tensor([v], dtype=torch.float64)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.SUM)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+def cuda_sync():
+    try:
+        import torch
+
+        if torch.cuda.is_available():
+            torch.cuda.synchronize()
+    except Exception:
+        pass
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,utilization.gpu,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = tempfile.mktemp(prefix="ela3d_clocks_", suffix=".csv")
+
+    def start(self):
+        try:
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.fh, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.fh.close()
+        rows = []
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 10:
+                continue
+            try:
+                rows.append({"sm": float(f[1]), "max": float(f[2]), "util": float(f[4]), "hw": f[6], "hwt": f[7],
+                             "swt": f[8], "pcap": f[9]})
+            except ValueError:
+                continue
+        os.unlink(self.path)
+        load = [r for r in rows if r["util"] >= 50] or rows
+        if not load:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        reasons = set()
+        for r in load:
+            for key, name in (("hw", "hw_slowdown"), ("hwt", "hw_thermal_slowdown"), ("swt", "sw_thermal_slowdown"),
+                              ("pcap", "sw_power_cap")):
+                if r[key].lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(r["sm"] for r in load), "sm_max_mhz": max(r["max"] for r in load),
+                "reasons": sorted(reasons), "samples": len(load)}
+
+
+def measured_peaks() -> tuple[float, str]:
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profile_traffic(kernel: str) -> float | None:
+    """DRAM bytes per launch from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", f"{kernel}_{WORKLOAD}.txt")
+    try:
+        for line in open(path):
+            if line.startswith("dram_bytes_per_launch_full_grid:"):
+                return float(line.split(":")[1])
+    except OSError:
+        pass
+    return None
+
+
+# ------------------------------------------------------------ workload --
+def workload(nstep: int = 2000):
+    from ela3d_gb300 import configs
+
+    return configs.anticline_256(nstep=nstep)
+
+
+def config_block(p, extra=None):
+    c = {"workload": f"{WORKLOAD}: {p.nx}x{p.ny}x{p.nz} cells, four-layer dome model, FP32, dt {p.dt} s, "
+                     f"{p.nstep}-step shot, {p.npml} PML cells, Ricker {p.f0:g} Hz on vz, {p.nrec} receivers",
+         "grid": [p.nx, p.ny, p.nz], "npml": p.npml, "nstep_shot": p.nstep,
+         "l2": "inputs larger than L2 (about 2.4 GB streamed per step vs 129 MB L2); no flush",
+         "parallelism": "one shot per GPU (shots are independent)"}
+    if extra:
+        c.update(extra)
+    return c
+
+
+# --------------------------------------------------------- CPU baseline --
+def cpu_reference_rate(p, cp, cs, rho, steps: int, procs: int) -> dict:
+    """Runs the reference CPU program (oracle/_ref) or, if it was not built,
+    the oracle's C restatement, as `procs` concurrent processes each doing
+    `steps` time steps of the shot; returns the aggregate rate."""
+    import oracle
+
+    exe = oracle.reference_binary(False)
+    cells = p.cells
+    warm = 1
+    wd = tempfile.mkdtemp(prefix="ela3d_cpu_")
+    try:
+        if exe:
+            for name, a in (("cp", cp), ("cs", cs), ("rho", rho)):
+                np.ascontiguousarray(a, np.float32).tofile(os.path.join(wd, f"m_{name}.bin"))
+            runs = []
+            for q in range(procs):
+                d = os.path.join(wd, f"r{q}")
+                os.makedirs(d)
+                oracle.write_config(os.path.join(d, "cfg.txt"), p.with_(nstep=steps + warm), steps + warm,
+                                    os.path.join(wd, "m_"), time_from=warm + 1)
+                runs.append((d, subprocess.Popen([exe, os.path.join(d, "cfg.txt")], cwd=d,
+                                                 stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)))
+            spans = []
+            for d, pr in runs:
+                if pr.wait() != 0:
+                    raise RuntimeError("reference program failed")
+                t0, t1, n = open(os.path.join(d, "steps.txt")).read().split()
+                spans.append((float(t0), float(t1), int(n)))
+            start = min(s[0] for s in spans)
+            end = max(s[1] for s in spans)
+            total = sum(cells * s[2] for s in spans)
+            kind = "reference"
+        else:
+            import multiprocessing as mp
+
+            ctx = mp.get_context("spawn")
+            with ctx.Pool(procs) as pool:
+                res = pool.starmap(_port_worker, [(p, cp, cs, rho, steps)] * procs)
+            start = min(r[0] for r in res)
+            end = max(r[1] for r in res)
+            total = cells * steps * procs
+            kind = "port"
+    finally:
+        import shutil
+
+        shutil.rmtree(wd, ignore_errors=True)
+    value = total / (end - start) / 1e9
+    return {"value": value, "unit": METRIC, "cores": procs, "kind": kind,
+            "sample": f"{procs} process(es) x {steps} time steps of the {p.nx}^3 shot "
+                      f"({'reference CPU program' if kind == 'reference' else 'C restatement'}), "
+                      f"{(end - start):.1f} s wall",
+            "seconds": end - start}
+
+
+def _port_worker(p, cp, cs, rho, steps):
+    import oracle
+
+    t0 = time.perf_counter()
+    oracle.run(p.with_(rec=np.zeros((0, 3), np.int32)), cp, cs, rho, steps, want_fields=False)
+    t1 = time.perf_counter()
+    return (t0, t1)
+
+
+# --------------------------------------------------------------- arms --
+def run_ours(args, rank, world, local):
+    import ela3d_gb300 as E
+    from ela3d_gb300.metrics import bytes_per_cell
+
+    E.select_device(local)
+    dist = Dist(world, True)
+    p, cp, cs, rho = workload()
+    cells = p.cells
+    clocks = ClockSampler(local)
+    plan = E.Plan(p, cp, cs, rho)
+    plan.run(args.warmup)
+    clocks.start()
+    plan.set_kernel_timing(True)
+    dist.barrier()
+    cuda_sync()
+    ms = plan.run_timed(args.steps)
+    cuda_sync()
+    dist.barrier()
+    s_ms, v_ms, ns, nv = plan.kernel_timing()
+    plan.set_kernel_timing(False)
+    plan.close()
+    t_max = dist.max(ms / 1e3)
+    value = cells * args.steps * world / t_max / 1e9
+
+    # e2e: one whole shot through the C ABI from host arrays
+    e2e = None
+    if not args.no_e2e:
+        dist.barrier()
+        t0 = time.perf_counter()
+        with E.Plan(p, cp, cs, rho) as shot:
+            shot.run(p.nstep)
+            seis = shot.seismograms()
+        t_e2e = dist.max(time.perf_counter() - t0)
+        e2e = {"value": cells * p.nstep * world / t_e2e / 1e9, "unit": METRIC,
+               "h2d_bytes_per_step": int(3 * cells * 4 / p.nstep),
+               "d2h_bytes_per_step": int(seis.nbytes / p.nstep),
+               "what": f"full {p.nstep}-step shot: plan creation with model upload, run, seismogram read-back",
+               "seconds": t_e2e}
+    clk = clocks.stop()
+
+    bpc = bytes_per_cell(p.nx, p.ny, p.nz, p.npml)
+    peak, peak_kind = measured_peaks()
+    kern = {}
+    for name, tot, n, b in (("stress_kernel", s_ms, ns, bpc["stress"]), ("velocity_kernel", v_ms, nv, bpc["velocity"])):
+        per = tot / max(n, 1) / 1e3
+        ach = b * cells / per / 1e9
+        kern[name] = {"launches": n, "mean_ms": per * 1e3, "bytes_per_launch": b * cells, "achieved_gbs": ach}
+    dom = max(kern, key=lambda k: kern[k]["mean_ms"])
+    traffic = profile_traffic(dom)
+    roof = {"bound": "hbm", "kernel": dom, "achieved": kern[dom]["achieved_gbs"], "peak": peak, "unit": "GB/s",
+            "frac": kern[dom]["achieved_gbs"] / peak, "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)",
+            "traffic": traffic, "bytes_per_cell_update": bpc["step"],
+            "step_achieved_gbs": bpc["step"] * cells * args.steps / (ms / 1e3) / 1e9,
+            "kernels": kern}
+    roof["step_frac"] = roof["step_achieved_gbs"] / peak
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        try:
+            cpu = cpu_reference_rate(p, cp, cs, rho, steps=args.cpu_steps, procs=1)
+        except Exception as e:  # reported, not fatal
+            cpu = {"value": None, "error": str(e)}
+    dist.close()
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": t_max * 1e3 / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic (seeded anticline model)",
+                "config": config_block(p, {"steps_timed": args.steps}),
+                "e2e": e2e, "gpu_launches": int(2 * args.steps * world), "roofline": roof,
+                "cpu_baseline": cpu, "clocks": clk}
+        print(json.dumps(line), flush=True)
+
+
+def run_reference(args, rank, world, local):
+    if rank != 0:
+        return
+    p, cp, cs, rho = workload()
+    procs = os.cpu_count() or 1
+    steps = max(1, min(args.steps, args.ref_steps_cap))
+    r = cpu_reference_rate(p, cp, cs, rho, steps=steps, procs=procs)
+    line = {"metric": METRIC, "value": r["value"], "unit": METRIC, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": r["seconds"] * 1e3 / steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded anticline model)",
+            "impl": "reference", "config": config_block(p, {"steps_timed": steps}),
+            "cpu_baseline": {k: r[k] for k in ("value", "unit", "cores", "kind", "sample")},
+            "e2e": {"value": r["value"], "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=400)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end shot (short profiling runs)")
+    ap.add_argument("--cpu-steps", type=int, default=20)
+    ap.add_argument("--ref-steps-cap", type=int, default=20)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        run_reference(args, rank, world, local)
+    else:
+        run_ours(args, rank, world, local)
+
+
+if __name__ == "__main__":
+    main()

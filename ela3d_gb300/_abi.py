@@ -38,6 +38,8 @@ SIGNATURES = [
     ("ela3d_get_kernel_timing", _c.c_int, [_P, _c.POINTER(_c.c_double), _c.POINTER(_c.c_double),
                                            _c.POINTER(_c.c_int64), _c.POINTER(_c.c_int64)]),
     ("ela3d_plan_destroy", _c.c_int, [_P]),
+    ("ela3d_select_device", _c.c_int, [_c.c_int32]),
+    ("ela3d_run_timed", _c.c_int, [_P, _c.c_int32, _c.POINTER(_c.c_double)]),
     ("ela3d_variant_count", _c.c_int32, []),
     ("ela3d_variant_get", _c.c_int, [_c.c_int32, _P]),
     ("ela3d_plan_create_tuned", _c.c_int, [_c.POINTER(CParams), _P, _P, _P, _P, _c.POINTER(_P)]),
@@ -97,6 +99,10 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
     return lib
 
 
+def select_device(ordinal: int) -> None:
+    _check(load_library().ela3d_select_device(ordinal), "ela3d_select_device")
+
+
 def _check(st: int, where: str) -> None:
     if st != 0:
         raise Ela3dError(st, where)
@@ -131,6 +137,13 @@ class Plan:
 
     def run(self, nsteps: int) -> None:
         _check(self._lib.ela3d_run(self._h, nsteps), "ela3d_run")
+
+    def run_timed(self, nsteps: int) -> float:
+        """Runs nsteps and returns their device time in ms (CUDA events on
+        the plan's stream)."""
+        ms = ctypes.c_double()
+        _check(self._lib.ela3d_run_timed(self._h, nsteps, ctypes.byref(ms)), "ela3d_run_timed")
+        return ms.value
 
     def enqueue(self, nsteps: int) -> None:
         _check(self._lib.ela3d_enqueue(self._h, nsteps), "ela3d_enqueue")

@@ -132,6 +132,22 @@ ela3d_status ela3d_plan_create(const ela3d_params *p, const float *cp, const flo
   return ela3d_plan_create_tuned(p, cp, cs, rho, nullptr, out);
 }
 
+ela3d_status ela3d_select_device(int32_t ordinal) {
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess) return status_from_cuda(e, "cudaGetDeviceCount");
+  if (ordinal < 0 || ordinal >= n) {
+    set_last_error("device ordinal out of range");
+    return ELA3D_ERR_INVALID_ARG;
+  }
+  return status_from_cuda(cudaSetDevice(ordinal), "cudaSetDevice");
+}
+
+ela3d_status ela3d_run_timed(ela3d_plan *plan, int32_t nsteps, double *ms) {
+  if (!plan || nsteps < 0) return ELA3D_ERR_INVALID_ARG;
+  return plan->eng->run_timed(nsteps, ms);
+}
+
 ela3d_status ela3d_enqueue(ela3d_plan *plan, int32_t nsteps) {
   if (!plan) return ELA3D_ERR_INVALID_ARG;
   return plan->eng->enqueue(nsteps);

@@ -127,11 +127,11 @@ TuneChoice default_choice(int fp64, int nx, int ny, int nz) {
   (void)nx; (void)ny; (void)nz;
   int n = 0;
   const Variant *v = variants(&n);
-  for (int i = 0; i < n; ++i) {
-    if (fp64 && v[i].fp64) return {i, 0, 16, 0};
-    if (!fp64 && !v[i].fp64) return {i, 0, 16, 0};
-  }
-  return {0, 0, 16, 0};
+  // first variant of the precision (the list is ordered best first for
+  // large grids), z-chunks of 16 planes dealt round-robin
+  for (int i = 0; i < n; ++i)
+    if ((v[i].fp64 != 0) == (fp64 != 0)) return {i, 1, 16, 0};
+  return {0, 1, 16, 0};
 }
 
 // ------------------------------------------------------------ TMA maps --
@@ -516,6 +516,22 @@ class Engine final : public EngineBase {
       if (st != ELA3D_OK) return st;
       ++tick_;
     }
+    return ELA3D_OK;
+  }
+
+  ela3d_status run_timed(int nsteps, double *ms) override {
+    cudaEvent_t a = event(), b = event();
+    CK(cudaEventRecord(a, stream_));
+    ela3d_status st = enqueue(nsteps);
+    if (st != ELA3D_OK) return st;
+    CK(cudaEventRecord(b, stream_));
+    st = sync();
+    if (st != ELA3D_OK) return st;
+    float t = 0.f;
+    CK(cudaEventElapsedTime(&t, a, b));
+    free_events_.push_back(a);
+    free_events_.push_back(b);
+    if (ms) *ms = t;
     return ELA3D_OK;
   }
 

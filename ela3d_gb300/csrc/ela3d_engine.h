@@ -55,6 +55,8 @@ class EngineBase {
                                 int shared_model_of) = 0;
   virtual ela3d_status finalize(const TuneChoice *choice) = 0;
   virtual ela3d_status enqueue(int nsteps) = 0;
+  // enqueue bracketed by events on the engine's stream; waits, returns ms
+  virtual ela3d_status run_timed(int nsteps, double *ms) = 0;
   virtual ela3d_status sync() = 0;
   virtual ela3d_status seismograms(int shot, void *out, int out_fp64) = 0;
   virtual ela3d_status field(int shot, int comp, void *out, int out_fp64) = 0;

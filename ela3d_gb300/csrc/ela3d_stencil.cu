@@ -15,7 +15,7 @@ static Variant make_variant() {
   v.tx = TX;
   v.ty = TY;
   v.ns = NS;
-  v.threads = G::NT;
+  v.threads = G::THREADS;
   v.stress_smem = G::S_SMEM;
   v.vel_smem = G::V_SMEM;
   v.halo = G::H;
@@ -25,13 +25,14 @@ static Variant make_variant() {
 }
 
 static const Variant kVariants[] = {
-    make_variant<float, 64, 8, 4>(),
-    make_variant<float, 64, 4, 4>(),
-    make_variant<float, 128, 4, 3>(),
-    make_variant<float, 32, 8, 4>(),
-    make_variant<float, 64, 16, 3>(),
-    make_variant<double, 32, 8, 3>(),
-    make_variant<double, 64, 4, 3>(),
+    make_variant<float, 128, 7, 4>(),
+    make_variant<float, 128, 6, 5>(),
+    make_variant<float, 128, 5, 6>(),
+    make_variant<float, 64, 14, 4>(),
+    make_variant<float, 128, 3, 4>(),
+    make_variant<float, 64, 6, 4>(),
+    make_variant<double, 32, 6, 3>(),
+    make_variant<double, 64, 3, 4>(),
 };
 
 const Variant *variants(int *count) {

@@ -3,19 +3,24 @@
 //
 // Scheme (2.5-D z-march, one launch per half-step):
 //  - a block owns a list of work items (shot, x-y tile, z-run [k0, k1));
-//  - for each plane k of an item, one elected thread issues TMA tiled loads
-//    of every input array's x-y tile (with the one-cell halos the stencil
-//    needs) into a ring of NS shared-memory stages, completing on an
-//    mbarrier per stage; out-of-grid halo cells arrive as zeros (the TMA
-//    fill), which is also the zero plane above k = nz-1 that the reference's
-//    sigma_xz/sigma_yz loop reads (simpelmodel.cpp:450,477);
-//  - the block computes plane k from stages k and k+1 (the z+1 neighbours)
-//    and keeps the z-1 neighbours in registers, each thread owning 16 bytes
-//    of consecutive x cells of one row (float4 / double2 accesses);
+//  - one producer warp walks the block's planes and, for each, issues TMA
+//    tiled loads of every input array's x-y tile (with the one-cell halos
+//    the stencil needs) into a ring of NS shared-memory stages; each stage
+//    has a "full" mbarrier (TMA bytes landed) and an "empty" mbarrier (all
+//    consumer warps done), so refills start as soon as a stage is released;
+//  - out-of-grid halo cells arrive as zeros (the TMA fill), which is also
+//    the zero plane above k = nz-1 that the reference's sigma_xz/sigma_yz
+//    loop reads (simpelmodel.cpp:450,477);
+//  - consumer warps compute plane k from stages k and k+1 (the z+1
+//    neighbours) and keep the z-1 neighbours in registers; each thread owns
+//    16 bytes of consecutive x cells of one row (float4 / double2);
 //  - C-PML memory variables are read and written only in the PML slabs;
 //  - cells outside the update ranges of the reference's loops keep their
-//    value (the Dirichlet edges), receivers are sampled after the velocity
+//    value (the Dirichlet edges); receivers are sampled after the velocity
 //    update and the force source is added after that (simpelmodel.cpp:592-622).
+// Every wait is bounded: on expiry the kernel ORs DEV_ERR_TIMEOUT into the
+// error word, the producer waits (bounded) for its issued copies, and the
+// threads return.
 #pragma once
 
 #include "ela3d_device.cuh"
@@ -28,9 +33,15 @@ struct Geo {
   static constexpr int H = VEC;          // halo width in x (16 bytes, the TMA x alignment)
   static constexpr int TX = TX_, TY = TY_, NS = NS_;
   static constexpr int NTX = TX / VEC;
-  static constexpr int NT = NTX * TY;
+  static constexpr int NT = NTX * TY;      // consumer threads
+  static constexpr int NCW = NT / 32;      // consumer warps
+  static constexpr int THREADS = NT + 32;  // + one producer warp
+  // blocks per SM the register budget is sized for: two blocks of four warps
+  // keep 255 registers per thread (64K registers, 16K per SM sub-partition)
+  static constexpr int MINB = THREADS <= 128 ? 2 : 1;
   static constexpr int WW = TX + H;
   static_assert(TX % VEC == 0 && TX + H <= 256 && TY + 1 <= 256, "tile shape");
+  static_assert(NT % 32 == 0, "consumer threads must fill whole warps");
   __host__ __device__ static constexpr int al(int b) { return (b + 127) & ~127; }
   static constexpr int C = TX * TY;          // center box
   static constexpr int W1 = WW * (TY + 1);   // wide box with one extra row
@@ -59,21 +70,10 @@ struct Geo {
   static constexpr int V_V = V_RHO + sz(W1);      // vx vy vz (C)
   static constexpr int V_STAGE = V_V + 3 * sz(C);
   static constexpr int V_TX = (int)sizeof(T) * (2 * W0 + 2 * Y1 + 4 * C + 2 * W1);
-  // mbarriers live after the stages, so the TMA destinations start at the
-  // (aligned) base of the block's dynamic shared memory
-  static constexpr int S_SMEM = NS * S_STAGE + 8 * NS;
-  static constexpr int V_SMEM = NS * V_STAGE + 8 * NS;
-};
-
-// Producer/consumer bookkeeping of the load sequence.  Every thread runs it
-// (it is a few integer operations per plane); thread 0 also issues the TMA.
-// Loads are numbered n = 0, 1, ...; load n goes to stage n % NS and its
-// mbarrier phase parity is (n / NS) & 1.  Item i contributes loads for
-// planes k0 .. k1 (k1 is the look-ahead plane, possibly nz = all zeros).
-struct LoadCursor {
-  int item, k;     // next plane to load
-  int end;         // item range end
-  long long n;     // loads issued
+  // mbarriers (full[NS], empty[NS]) live after the stages, so the TMA
+  // destinations start at the (aligned) base of dynamic shared memory
+  static constexpr int S_SMEM = NS * S_STAGE + 16 * NS;
+  static constexpr int V_SMEM = NS * V_STAGE + 16 * NS;
 };
 
 template <typename T>
@@ -81,9 +81,45 @@ __device__ __forceinline__ int tiles_x_of(const ShotDesc<T> &s, int TX) {
   return (s.nx + TX - 1) / TX;
 }
 
+// dt / rho_avg: FP32 uses the hardware reciprocal-based divide (<= 2 ulp
+// from the IEEE quotient); FP64 keeps the IEEE division.
+__device__ __forceinline__ float div_fast(float a, float b) { return __fdividef(a, b); }
+__device__ __forceinline__ double div_fast(double a, double b) { return a / b; }
+
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+// Producer: one thread walks the block's items and issues every plane's
+// loads.  Load n goes to stage n % NS; before reusing a stage it waits for
+// the consumers' release of load n - NS on that stage's empty barrier.
+// Item i contributes planes k0 .. k1 (k1 is the look-ahead plane, possibly
+// nz, which the TMA fills with zeros).
+template <int NS, typename Issue>
+__device__ __forceinline__ void produce(const Item *__restrict__ items, int2 range, uint64_t *full, uint64_t *empty,
+                                        Issue issue, unsigned *__restrict__ err) {
+  long long n = 0;
+  bool ok = true;
+  for (int ii = range.x; ii < range.y && ok; ++ii) {
+    const Item it = items[ii];
+    for (int k = it.k0; k <= it.k1; ++k, ++n) {
+      const int slot = (int)(n % NS);
+      if (n >= NS && !mbar_wait_bounded(&empty[slot], (uint32_t)(((n / NS) - 1) & 1))) {
+        ok = false;
+        break;
+      }
+      issue(it, k, slot, &full[slot]);
+    }
+  }
+  if (!ok) atomicOr(err, DEV_ERR_TIMEOUT);
+  // the block must not exit with copies in flight
+  for (long long q = (n > NS ? n - NS : 0); q < n; ++q)
+    mbar_wait_bounded(&full[q % NS], (uint32_t)((q / NS) & 1), 200000000ull);
+}
+
 // ----------------------------------------------------------- stress ----
 template <typename T, int TX, int TY, int NS>
-__global__ void __launch_bounds__(Geo<T, TX, TY, NS>::NT)
+__global__ void __launch_bounds__(Geo<T, TX, TY, NS>::THREADS, Geo<T, TX, TY, NS>::MINB)
     stress_kernel(const ShotDesc<T> *__restrict__ shots, const ShotMaps *__restrict__ maps,
                   const Item *__restrict__ items, const int2 *__restrict__ ranges, int tick,
                   unsigned *__restrict__ err) {
@@ -91,65 +127,71 @@ __global__ void __launch_bounds__(Geo<T, TX, TY, NS>::NT)
   constexpr int V = G::VEC, H = G::H, WW = G::WW;
   extern __shared__ __align__(1024) unsigned char smem[];
   uint64_t *full = reinterpret_cast<uint64_t *>(smem + NS * G::S_STAGE);
+  uint64_t *empty = full + NS;
 
   const int tid = threadIdx.x;
-  const int tx = tid % G::NTX, ty = tid / G::NTX;
   const int2 range = ranges[blockIdx.x];
   if (range.x >= range.y) return;
 
   if (tid == 0) {
-    for (int s = 0; s < NS; ++s) mbar_init(&full[s], 1);
+    for (int s = 0; s < NS; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], G::NCW);
+    }
     fence_mbar_init();
   }
   __syncthreads();
 
-  LoadCursor pc{range.x, items[range.x].k0, range.y, 0};
-  auto issue = [&](bool do_copy) {
-    const Item it = items[pc.item];
-    const int txs = tiles_x_of(shots[it.shot], TX);
-    const int x0 = (it.tile % txs) * TX, y0 = (it.tile / txs) * TY;
-    const int slot = (int)(pc.n % NS);
-    if (do_copy) {
-      unsigned char *st = smem + slot * G::S_STAGE;
-      const CUtensorMap *m = maps[it.shot].stress;
-      uint64_t *bar = &full[slot];
-      mbar_arrive_expect_tx(bar, G::S_TX);
-      tma_load_3d(st + G::S_VX, &m[0], x0, y0, pc.k, bar);
-      tma_load_3d(st + G::S_VY, &m[1], x0 - H, y0 - 1, pc.k, bar);
-      tma_load_3d(st + G::S_VZ, &m[2], x0 - H, y0, pc.k, bar);
-      tma_load_3d(st + G::S_CS, &m[3], x0 - H, y0, pc.k, bar);
-      tma_load_3d(st + G::S_RHO, &m[4], x0 - H, y0, pc.k, bar);
-      tma_load_3d(st + G::S_CP, &m[5], x0, y0, pc.k, bar);
+  if (tid >= G::NT) {  // producer warp
+    if (tid == G::NT) {
+      auto issue = [&](const Item &it, int k, int slot, uint64_t *bar) {
+        const int txs = tiles_x_of(shots[it.shot], TX);
+        const int x0 = (it.tile % txs) * TX, y0 = (it.tile / txs) * TY;
+        unsigned char *st = smem + slot * G::S_STAGE;
+        const CUtensorMap *m = maps[it.shot].stress;
+        mbar_arrive_expect_tx(bar, G::S_TX);
+        tma_load_3d(st + G::S_VX, &m[0], x0, y0, k, bar);
+        tma_load_3d(st + G::S_VY, &m[1], x0 - H, y0 - 1, k, bar);
+        tma_load_3d(st + G::S_VZ, &m[2], x0 - H, y0, k, bar);
+        tma_load_3d(st + G::S_CS, &m[3], x0 - H, y0, k, bar);
+        tma_load_3d(st + G::S_RHO, &m[4], x0 - H, y0, k, bar);
+        tma_load_3d(st + G::S_CP, &m[5], x0, y0, k, bar);
 #pragma unroll
-      for (int c = 0; c < 6; ++c)
-        tma_load_3d(st + G::S_SIG + c * G::SC, &m[6 + c], x0, y0, pc.k, bar);
+        for (int c = 0; c < 6; ++c) tma_load_3d(st + G::S_SIG + c * G::SC, &m[6 + c], x0, y0, k, bar);
+      };
+      produce<NS>(items, range, full, empty, issue, err);
     }
-    ++pc.n;
-    if (++pc.k > it.k1) {
-      if (++pc.item < pc.end) pc.k = items[pc.item].k0;
-    }
-  };
-  for (int s = 0; s < NS && pc.item < pc.end; ++s) issue(tid == 0);
+    return;
+  }
 
-  long long consumed = 0;
-  bool timed_out = false;
+  const int lane = tid & 31;
+  const int tx = tid % G::NTX, ty = tid / G::NTX;
+  long long n = 0;  // index of the load holding the current plane
 
   for (int ii = range.x; ii < range.y; ++ii) {
     const Item item = items[ii];
     const ShotDesc<T> &sd = shots[item.shot];
     const int nx = sd.nx, ny = sd.ny, nz = sd.nz, px = sd.px;
-    const int txs = tiles_x_of(sd, TX);
+    const int txs = (nx + TX - 1) / TX;
     const int x0 = (item.tile % txs) * TX, y0 = (item.tile / txs) * TY;
     const int xg = x0 + tx * V, y = y0 + ty;
     const bool live = (xg < nx) && (y < ny);
     const T dt = sd.dt, idx = sd.idx, idy = sd.idy, idz = sd.idz;
     const long long plane = (long long)ny * px;
+    const long long rowoff = (long long)y * px + xg;
+    T *const f3 = sd.f[3], *const f4 = sd.f[4], *const f5 = sd.f[5];
+    T *const f6 = sd.f[6], *const f7 = sd.f[7], *const f8 = sd.f[8];
+    const int zl = sd.zl, zr = sd.zr;
+    const T *const prof_z = sd.prof_z;
+    T *const psi_x = sd.psi_x, *const psi_y = sd.psi_y, *const psi_z = sd.psi_z;
+    const long long psx = sd.psx, psy = sd.psy, psz = sd.psz;
+    const int xw = sd.xw, yw = sd.yw;
 
     // z-1 neighbour of vz for the first plane of the run
     T vz_zm[V];
 #pragma unroll
     for (int e = 0; e < V; ++e) vz_zm[e] = T(0);
-    if (live && item.k0 > 0) ld_vec_rw(sd.f[2] + (long long)(item.k0 - 1) * plane + (long long)y * px + xg, vz_zm);
+    if (live && item.k0 > 0) ld_vec_rw(sd.f[2] + (long long)(item.k0 - 1) * plane + rowoff, vz_zm);
 
     // x-slab profile and placement (fixed over the run)
     const bool in_x = live && (xg < sd.xl || xg >= sd.xr);
@@ -179,11 +221,50 @@ __global__ void __launch_bounds__(Geo<T, TX, TY, NS>::NT)
     const int sc = ty * TX + tx * V;         // centre boxes
 
     for (int k = item.k0; k < item.k1; ++k) {
-      const long long n = consumed;
+      // memory variables and z profile first: their latency overlaps the wait
+      const bool in_z = live && (k < zl || k >= zr);
+      const int zs = k < zl ? k : zl + (k - zr);
+      T az = 0, bz = 1, ikz = 1, azh = 0, bzh = 1, ikzh = 1;
+      if (in_z) {
+        az = prof_z[PR_A * nz + k]; bz = prof_z[PR_B * nz + k]; ikz = prof_z[PR_IK * nz + k];
+        azh = prof_z[PR_AH * nz + k]; bzh = prof_z[PR_BH * nz + k]; ikzh = prof_z[PR_IKH * nz + k];
+      }
+      T px0[V], px1[V], px2[V], py0[V], py1[V], py2[V], pz0[V], pz1[V], pz2[V];
+      T *gx = psi_x + ((long long)k * ny + y) * xw + xs;
+      T *gy = psi_y + ((long long)k * yw + ys) * px + xg;
+      T *gz = psi_z + ((long long)zs * ny + y) * px + xg;
+      if (in_x) {
+        ld_vec_rw(gx + PSI_S0 * psx, px0);
+        ld_vec_rw(gx + PSI_S1 * psx, px1);
+        ld_vec_rw(gx + PSI_S2 * psx, px2);
+      } else {
+#pragma unroll
+        for (int e = 0; e < V; ++e) px0[e] = px1[e] = px2[e] = T(0);
+      }
+      if (in_y) {
+        ld_vec_rw(gy + PSI_S0 * psy, py0);
+        ld_vec_rw(gy + PSI_S1 * psy, py1);
+        ld_vec_rw(gy + PSI_S2 * psy, py2);
+      } else {
+#pragma unroll
+        for (int e = 0; e < V; ++e) py0[e] = py1[e] = py2[e] = T(0);
+      }
+      if (in_z) {
+        ld_vec_rw(gz + PSI_S0 * psz, pz0);
+        ld_vec_rw(gz + PSI_S1 * psz, pz1);
+        ld_vec_rw(gz + PSI_S2 * psz, pz2);
+      } else {
+#pragma unroll
+        for (int e = 0; e < V; ++e) pz0[e] = pz1[e] = pz2[e] = T(0);
+      }
+
       const int s0 = (int)(n % NS), s1 = (int)((n + 1) % NS);
       bool ok = mbar_wait_bounded(&full[s0], (uint32_t)((n / NS) & 1));
       ok = ok && mbar_wait_bounded(&full[s1], (uint32_t)(((n + 1) / NS) & 1));
-      timed_out |= !ok;
+      if (__any_sync(0xffffffffu, !ok)) {
+        if (lane == 0) atomicOr(err, DEV_ERR_TIMEOUT);
+        return;
+      }
       const unsigned char *cur = smem + s0 * G::S_STAGE;
       const unsigned char *nxt = smem + s1 * G::S_STAGE;
       const T *bvx = reinterpret_cast<const T *>(cur + G::S_VX);
@@ -193,6 +274,7 @@ __global__ void __launch_bounds__(Geo<T, TX, TY, NS>::NT)
       const T *brho = reinterpret_cast<const T *>(cur + G::S_RHO);
       const T *bcp = reinterpret_cast<const T *>(cur + G::S_CP);
       const T *bsig = reinterpret_cast<const T *>(cur + G::S_SIG);
+      constexpr int CS = G::SC / (int)sizeof(T);
 
       T vx_c[V], vx_yp[V], vx_zp[V], vy_c[V], vy_ym[V], vy_zp[V], vz_c[V], vz_yp[V];
       T cs_c[V], cs_yp[V], cs_zp[V], rho_c[V], rho_yp[V], rho_zp[V], cp_c[V];
@@ -217,49 +299,19 @@ __global__ void __launch_bounds__(Geo<T, TX, TY, NS>::NT)
       ld_vec(reinterpret_cast<const T *>(nxt + G::S_RHO) + sl, rho_zp);
       ld_vec(bcp + sc, cp_c);
       T sxx[V], syy[V], szz[V], sxy[V], sxz[V], syz[V];
-      ld_vec(bsig + 0 * (G::SC / (int)sizeof(T)) + sc, sxx);
-      ld_vec(bsig + 1 * (G::SC / (int)sizeof(T)) + sc, syy);
-      ld_vec(bsig + 2 * (G::SC / (int)sizeof(T)) + sc, szz);
-      ld_vec(bsig + 3 * (G::SC / (int)sizeof(T)) + sc, sxy);
-      ld_vec(bsig + 4 * (G::SC / (int)sizeof(T)) + sc, sxz);
-      ld_vec(bsig + 5 * (G::SC / (int)sizeof(T)) + sc, syz);
+      ld_vec(bsig + 0 * CS + sc, sxx);
+      ld_vec(bsig + 1 * CS + sc, syy);
+      ld_vec(bsig + 2 * CS + sc, szz);
+      ld_vec(bsig + 3 * CS + sc, sxy);
+      ld_vec(bsig + 4 * CS + sc, sxz);
+      ld_vec(bsig + 5 * CS + sc, syz);
 
-      const bool in_z = live && (k < sd.zl || k >= sd.zr);
-      const int zs = k < sd.zl ? k : sd.zl + (k - sd.zr);
-      T az = 0, bz = 1, ikz = 1, azh = 0, bzh = 1, ikzh = 1;
-      if (in_z) {
-        az = sd.prof_z[PR_A * nz + k]; bz = sd.prof_z[PR_B * nz + k]; ikz = sd.prof_z[PR_IK * nz + k];
-        azh = sd.prof_z[PR_AH * nz + k]; bzh = sd.prof_z[PR_BH * nz + k]; ikzh = sd.prof_z[PR_IKH * nz + k];
-      }
-      // psi of this group (zero when outside a slab)
-      T px0[V], px1[V], px2[V], py0[V], py1[V], py2[V], pz0[V], pz1[V], pz2[V];
-      T *gx = nullptr, *gy = nullptr, *gz = nullptr;
-      if (in_x) {
-        gx = sd.psi_x + ((long long)k * ny + y) * sd.xw + xs;
-        ld_vec_rw(gx + PSI_S0 * sd.psx, px0);
-        ld_vec_rw(gx + PSI_S1 * sd.psx, px1);
-        ld_vec_rw(gx + PSI_S2 * sd.psx, px2);
-      } else {
-#pragma unroll
-        for (int e = 0; e < V; ++e) px0[e] = px1[e] = px2[e] = T(0);
-      }
-      if (in_y) {
-        gy = sd.psi_y + ((long long)k * sd.yw + ys) * px + xg;
-        ld_vec_rw(gy + PSI_S0 * sd.psy, py0);
-        ld_vec_rw(gy + PSI_S1 * sd.psy, py1);
-        ld_vec_rw(gy + PSI_S2 * sd.psy, py2);
-      } else {
-#pragma unroll
-        for (int e = 0; e < V; ++e) py0[e] = py1[e] = py2[e] = T(0);
-      }
-      if (in_z) {
-        gz = sd.psi_z + ((long long)zs * ny + y) * px + xg;
-        ld_vec_rw(gz + PSI_S0 * sd.psz, pz0);
-        ld_vec_rw(gz + PSI_S1 * sd.psz, pz1);
-        ld_vec_rw(gz + PSI_S2 * sd.psz, pz2);
-      } else {
-#pragma unroll
-        for (int e = 0; e < V; ++e) pz0[e] = pz1[e] = pz2[e] = T(0);
+      // stage s0 is no longer read by this warp (s1 still is, as the next plane)
+      const bool last = (k == item.k1 - 1);
+      __syncwarp();
+      if (lane == 0) {
+        mbar_arrive(&empty[s0]);
+        if (last) mbar_arrive(&empty[s1]);
       }
 
       const bool yN = (y >= 1) && (k >= 1);   // normal stresses: j >= 2, k >= 2 (1-based)
@@ -351,47 +403,37 @@ __global__ void __launch_bounds__(Geo<T, TX, TY, NS>::NT)
       }
 
       if (live) {
-        const long long g = (long long)k * plane + (long long)y * px + xg;
-        st_vec(sd.f[3] + g, sxx);
-        st_vec(sd.f[4] + g, syy);
-        st_vec(sd.f[5] + g, szz);
-        st_vec(sd.f[6] + g, sxy);
-        st_vec(sd.f[7] + g, sxz);
-        st_vec(sd.f[8] + g, syz);
+        const long long g = (long long)k * plane + rowoff;
+        st_vec(f3 + g, sxx);
+        st_vec(f4 + g, syy);
+        st_vec(f5 + g, szz);
+        st_vec(f6 + g, sxy);
+        st_vec(f7 + g, sxz);
+        st_vec(f8 + g, syz);
         if (in_x) {
-          st_vec(gx + PSI_S0 * sd.psx, px0);
-          st_vec(gx + PSI_S1 * sd.psx, px1);
-          st_vec(gx + PSI_S2 * sd.psx, px2);
+          st_vec(gx + PSI_S0 * psx, px0);
+          st_vec(gx + PSI_S1 * psx, px1);
+          st_vec(gx + PSI_S2 * psx, px2);
         }
         if (in_y) {
-          st_vec(gy + PSI_S0 * sd.psy, py0);
-          st_vec(gy + PSI_S1 * sd.psy, py1);
-          st_vec(gy + PSI_S2 * sd.psy, py2);
+          st_vec(gy + PSI_S0 * psy, py0);
+          st_vec(gy + PSI_S1 * psy, py1);
+          st_vec(gy + PSI_S2 * psy, py2);
         }
         if (in_z) {
-          st_vec(gz + PSI_S0 * sd.psz, pz0);
-          st_vec(gz + PSI_S1 * sd.psz, pz1);
-          st_vec(gz + PSI_S2 * sd.psz, pz2);
+          st_vec(gz + PSI_S0 * psz, pz0);
+          st_vec(gz + PSI_S1 * psz, pz1);
+          st_vec(gz + PSI_S2 * psz, pz2);
         }
       }
-
-      // every thread is done with stage n (and n+1 at the end of the run)
-      if (__syncthreads_or(timed_out)) {
-        if (tid == 0) atomicOr(err, DEV_ERR_TIMEOUT);
-        // let the loads already issued land before the block exits
-        for (long long q = consumed; q < pc.n; ++q)
-          mbar_wait_bounded(&full[q % NS], (uint32_t)((q / NS) & 1), 100000000ull);
-        return;
-      }
-      consumed += (k == item.k1 - 1) ? 2 : 1;
-      while (pc.item < pc.end && pc.n < consumed + NS) issue(tid == 0);
+      n += last ? 2 : 1;
     }
   }
 }
 
 // --------------------------------------------------------- velocity ----
 template <typename T, int TX, int TY, int NS>
-__global__ void __launch_bounds__(Geo<T, TX, TY, NS>::NT)
+__global__ void __launch_bounds__(Geo<T, TX, TY, NS>::THREADS, Geo<T, TX, TY, NS>::MINB)
     velocity_kernel(const ShotDesc<T> *__restrict__ shots, const ShotMaps *__restrict__ maps,
                     const Item *__restrict__ items, const int2 *__restrict__ ranges, int tick,
                     unsigned *__restrict__ err) {
@@ -399,70 +441,78 @@ __global__ void __launch_bounds__(Geo<T, TX, TY, NS>::NT)
   constexpr int V = G::VEC, H = G::H, WW = G::WW;
   extern __shared__ __align__(1024) unsigned char smem[];
   uint64_t *full = reinterpret_cast<uint64_t *>(smem + NS * G::V_STAGE);
+  uint64_t *empty = full + NS;
 
   const int tid = threadIdx.x;
-  const int tx = tid % G::NTX, ty = tid / G::NTX;
   const int2 range = ranges[blockIdx.x];
   if (range.x >= range.y) return;
 
   if (tid == 0) {
-    for (int s = 0; s < NS; ++s) mbar_init(&full[s], 1);
+    for (int s = 0; s < NS; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], G::NCW);
+    }
     fence_mbar_init();
   }
   __syncthreads();
 
-  LoadCursor pc{range.x, items[range.x].k0, range.y, 0};
-  auto issue = [&](bool do_copy) {
-    const Item it = items[pc.item];
-    const int txs = tiles_x_of(shots[it.shot], TX);
-    const int x0 = (it.tile % txs) * TX, y0 = (it.tile / txs) * TY;
-    const int slot = (int)(pc.n % NS);
-    if (do_copy) {
-      unsigned char *st = smem + slot * G::V_STAGE;
-      const CUtensorMap *m = maps[it.shot].vel;
-      uint64_t *bar = &full[slot];
-      mbar_arrive_expect_tx(bar, G::V_TX);
-      tma_load_3d(st + G::V_SXX, &m[0], x0 - H, y0, pc.k, bar);
-      tma_load_3d(st + G::V_SYY, &m[1], x0, y0, pc.k, bar);
-      tma_load_3d(st + G::V_SZZ, &m[2], x0, y0, pc.k, bar);
-      tma_load_3d(st + G::V_SXY, &m[3], x0, y0 - 1, pc.k, bar);
-      tma_load_3d(st + G::V_SXZ, &m[4], x0, y0, pc.k, bar);
-      tma_load_3d(st + G::V_SYZ, &m[5], x0, y0 - 1, pc.k, bar);
-      tma_load_3d(st + G::V_RHO, &m[6], x0 - H, y0, pc.k, bar);
+  if (tid >= G::NT) {  // producer warp
+    if (tid == G::NT) {
+      auto issue = [&](const Item &it, int k, int slot, uint64_t *bar) {
+        const int txs = tiles_x_of(shots[it.shot], TX);
+        const int x0 = (it.tile % txs) * TX, y0 = (it.tile / txs) * TY;
+        unsigned char *st = smem + slot * G::V_STAGE;
+        const CUtensorMap *m = maps[it.shot].vel;
+        mbar_arrive_expect_tx(bar, G::V_TX);
+        tma_load_3d(st + G::V_SXX, &m[0], x0 - H, y0, k, bar);
+        tma_load_3d(st + G::V_SYY, &m[1], x0, y0, k, bar);
+        tma_load_3d(st + G::V_SZZ, &m[2], x0, y0, k, bar);
+        tma_load_3d(st + G::V_SXY, &m[3], x0, y0 - 1, k, bar);
+        tma_load_3d(st + G::V_SXZ, &m[4], x0, y0, k, bar);
+        tma_load_3d(st + G::V_SYZ, &m[5], x0, y0 - 1, k, bar);
+        tma_load_3d(st + G::V_RHO, &m[6], x0 - H, y0, k, bar);
 #pragma unroll
-      for (int c = 0; c < 3; ++c)
-        tma_load_3d(st + G::V_V + c * G::SC, &m[7 + c], x0, y0, pc.k, bar);
+        for (int c = 0; c < 3; ++c) tma_load_3d(st + G::V_V + c * G::SC, &m[7 + c], x0, y0, k, bar);
+      };
+      produce<NS>(items, range, full, empty, issue, err);
     }
-    ++pc.n;
-    if (++pc.k > it.k1) {
-      if (++pc.item < pc.end) pc.k = items[pc.item].k0;
-    }
-  };
-  for (int s = 0; s < NS && pc.item < pc.end; ++s) issue(tid == 0);
+    return;
+  }
 
-  long long consumed = 0;
-  bool timed_out = false;
+  const int lane = tid & 31;
+  const int tx = tid % G::NTX, ty = tid / G::NTX;
   constexpr int CS = G::SC / (int)sizeof(T);
+  long long n = 0;
 
   for (int ii = range.x; ii < range.y; ++ii) {
     const Item item = items[ii];
     const ShotDesc<T> &sd = shots[item.shot];
     const int nx = sd.nx, ny = sd.ny, nz = sd.nz, px = sd.px;
-    const int txs = tiles_x_of(sd, TX);
+    const int txs = (nx + TX - 1) / TX;
     const int x0 = (item.tile % txs) * TX, y0 = (item.tile / txs) * TY;
     const int xg = x0 + tx * V, y = y0 + ty;
     const bool live = (xg < nx) && (y < ny);
     const T dt = sd.dt, idx = sd.idx, idy = sd.idy, idz = sd.idz;
     const long long plane = (long long)ny * px;
+    const long long rowoff = (long long)y * px + xg;
+    T *const f0 = sd.f[0], *const f1 = sd.f[1], *const f2 = sd.f[2];
+    const int zl = sd.zl, zr = sd.zr;
+    const T *const prof_z = sd.prof_z;
+    T *const psi_x = sd.psi_x, *const psi_y = sd.psi_y, *const psi_z = sd.psi_z;
+    const long long psx = sd.psx, psy = sd.psy, psz = sd.psz;
+    const int xw = sd.xw, yw = sd.yw;
     const int it_step = tick - sd.tick0;
     const bool sample = (it_step % sd.sampgat == 0) && (it_step / sd.sampgat <= sd.nsamp) && it_step > 0;
     const int samp = it_step / sd.sampgat - 1;
+    const int *const rec_plane = sd.rec_plane;
+    const bool src_row = sd.src_kind == 0 && y == sd.src_j && sd.src_i >= xg && sd.src_i < xg + V &&
+                         it_step >= 1 && it_step <= sd.nstep;
 
     T sxz_zm[V], syz_zm[V];
 #pragma unroll
     for (int e = 0; e < V; ++e) sxz_zm[e] = syz_zm[e] = T(0);
     if (live && item.k0 > 0) {
-      const long long g = (long long)(item.k0 - 1) * plane + (long long)y * px + xg;
+      const long long g = (long long)(item.k0 - 1) * plane + rowoff;
       ld_vec_rw(sd.f[7] + g, sxz_zm);
       ld_vec_rw(sd.f[8] + g, syz_zm);
     }
@@ -495,11 +545,55 @@ __global__ void __launch_bounds__(Geo<T, TX, TY, NS>::NT)
     const int sc1 = (ty + 1) * TX + tx * V;   // syz box (origin x0, y0-1)
 
     for (int k = item.k0; k < item.k1; ++k) {
-      const long long n = consumed;
+      const bool in_z = live && (k < zl || k >= zr);
+      const int zs = k < zl ? k : zl + (k - zr);
+      T az = 0, bz = 1, ikz = 1, azh = 0, bzh = 1, ikzh = 1;
+      if (in_z) {
+        az = prof_z[PR_A * nz + k]; bz = prof_z[PR_B * nz + k]; ikz = prof_z[PR_IK * nz + k];
+        azh = prof_z[PR_AH * nz + k]; bzh = prof_z[PR_BH * nz + k]; ikzh = prof_z[PR_IKH * nz + k];
+      }
+      T px0[V], px1[V], px2[V], py0[V], py1[V], py2[V], pz0[V], pz1[V], pz2[V];
+      T *gx = psi_x + ((long long)k * ny + y) * xw + xs;
+      T *gy = psi_y + ((long long)k * yw + ys) * px + xg;
+      T *gz = psi_z + ((long long)zs * ny + y) * px + xg;
+      if (in_x) {
+        ld_vec_rw(gx + PSI_V0 * psx, px0);
+        ld_vec_rw(gx + PSI_V1 * psx, px1);
+        ld_vec_rw(gx + PSI_V2 * psx, px2);
+      } else {
+#pragma unroll
+        for (int e = 0; e < V; ++e) px0[e] = px1[e] = px2[e] = T(0);
+      }
+      if (in_y) {
+        ld_vec_rw(gy + PSI_V0 * psy, py0);
+        ld_vec_rw(gy + PSI_V1 * psy, py1);
+        ld_vec_rw(gy + PSI_V2 * psy, py2);
+      } else {
+#pragma unroll
+        for (int e = 0; e < V; ++e) py0[e] = py1[e] = py2[e] = T(0);
+      }
+      if (in_z) {
+        ld_vec_rw(gz + PSI_V0 * psz, pz0);
+        ld_vec_rw(gz + PSI_V1 * psz, pz1);
+        ld_vec_rw(gz + PSI_V2 * psz, pz2);
+      } else {
+#pragma unroll
+        for (int e = 0; e < V; ++e) pz0[e] = pz1[e] = pz2[e] = T(0);
+      }
+
+      int rlo = 0, rhi = 0;   // receivers of this plane
+      if (sample) {
+        rlo = rec_plane[k];
+        rhi = rec_plane[k + 1];
+      }
+
       const int s0 = (int)(n % NS), s1 = (int)((n + 1) % NS);
       bool ok = mbar_wait_bounded(&full[s0], (uint32_t)((n / NS) & 1));
       ok = ok && mbar_wait_bounded(&full[s1], (uint32_t)(((n + 1) / NS) & 1));
-      timed_out |= !ok;
+      if (__any_sync(0xffffffffu, !ok)) {
+        if (lane == 0) atomicOr(err, DEV_ERR_TIMEOUT);
+        return;
+      }
       const unsigned char *cur = smem + s0 * G::V_STAGE;
       const unsigned char *nxt = smem + s1 * G::V_STAGE;
       const T *bsxx = reinterpret_cast<const T *>(cur + G::V_SXX);
@@ -534,41 +628,11 @@ __global__ void __launch_bounds__(Geo<T, TX, TY, NS>::NT)
       ld_vec(bv + 1 * CS + sc, vy);
       ld_vec(bv + 2 * CS + sc, vz);
 
-      const bool in_z = live && (k < sd.zl || k >= sd.zr);
-      const int zs = k < sd.zl ? k : sd.zl + (k - sd.zr);
-      T az = 0, bz = 1, ikz = 1, azh = 0, bzh = 1, ikzh = 1;
-      if (in_z) {
-        az = sd.prof_z[PR_A * nz + k]; bz = sd.prof_z[PR_B * nz + k]; ikz = sd.prof_z[PR_IK * nz + k];
-        azh = sd.prof_z[PR_AH * nz + k]; bzh = sd.prof_z[PR_BH * nz + k]; ikzh = sd.prof_z[PR_IKH * nz + k];
-      }
-      T px0[V], px1[V], px2[V], py0[V], py1[V], py2[V], pz0[V], pz1[V], pz2[V];
-      T *gx = nullptr, *gy = nullptr, *gz = nullptr;
-      if (in_x) {
-        gx = sd.psi_x + ((long long)k * ny + y) * sd.xw + xs;
-        ld_vec_rw(gx + PSI_V0 * sd.psx, px0);
-        ld_vec_rw(gx + PSI_V1 * sd.psx, px1);
-        ld_vec_rw(gx + PSI_V2 * sd.psx, px2);
-      } else {
-#pragma unroll
-        for (int e = 0; e < V; ++e) px0[e] = px1[e] = px2[e] = T(0);
-      }
-      if (in_y) {
-        gy = sd.psi_y + ((long long)k * sd.yw + ys) * px + xg;
-        ld_vec_rw(gy + PSI_V0 * sd.psy, py0);
-        ld_vec_rw(gy + PSI_V1 * sd.psy, py1);
-        ld_vec_rw(gy + PSI_V2 * sd.psy, py2);
-      } else {
-#pragma unroll
-        for (int e = 0; e < V; ++e) py0[e] = py1[e] = py2[e] = T(0);
-      }
-      if (in_z) {
-        gz = sd.psi_z + ((long long)zs * ny + y) * px + xg;
-        ld_vec_rw(gz + PSI_V0 * sd.psz, pz0);
-        ld_vec_rw(gz + PSI_V1 * sd.psz, pz1);
-        ld_vec_rw(gz + PSI_V2 * sd.psz, pz2);
-      } else {
-#pragma unroll
-        for (int e = 0; e < V; ++e) pz0[e] = pz1[e] = pz2[e] = T(0);
+      const bool last = (k == item.k1 - 1);
+      __syncwarp();
+      if (lane == 0) {
+        mbar_arrive(&empty[s0]);
+        if (last) mbar_arrive(&empty[s1]);
       }
 
       const bool mvx_yz = (y >= 1) && (k >= 1);
@@ -587,7 +651,7 @@ __global__ void __launch_bounds__(Geo<T, TX, TY, NS>::NT)
           const bool m = mvx_yz && (x >= 1) && (x <= nx - 1);
           const T rhos = (rho_c[e] + rho_xm) / T(2);
           rbx[e] = rhos;
-          const T DT_over_rho = dt / rhos;
+          const T DT_over_rho = div_fast(dt, rhos);
           T d1 = (sxx_c[e] - sxx_xm) * idx;
           T d2 = (sxy_c[e] - sxy_ym[e]) * idy;
           T d3 = (sxz_c[e] - sxz_zm[e]) * idz;
@@ -607,7 +671,7 @@ __global__ void __launch_bounds__(Geo<T, TX, TY, NS>::NT)
           const bool m = mvy_yz && (x <= nx - 2);
           const T rhos = (rho_c[e] + rho_yp[e]) / T(2);
           rby[e] = rhos;
-          const T DT_over_rho = dt / rhos;
+          const T DT_over_rho = div_fast(dt, rhos);
           T d1 = (sxy_xp - sxy_c[e]) * idx;
           T d2 = (syy_yp[e] - syy_c[e]) * idy;
           T d3 = (syz_c[e] - syz_zm[e]) * idz;
@@ -627,7 +691,7 @@ __global__ void __launch_bounds__(Geo<T, TX, TY, NS>::NT)
           const bool m = mvz_yz && (x <= nx - 2);
           const T rhos = (rho_c[e] + rho_zp[e]) / T(2);
           rbz[e] = rhos;
-          const T DT_over_rho = dt / rhos;
+          const T DT_over_rho = div_fast(dt, rhos);
           T d1 = (sxz_xp - sxz_c[e]) * idx;
           T d2 = (syz_c[e] - syz_ym[e]) * idy;
           T d3 = (szz_zp[e] - szz_c[e]) * idz;
@@ -648,15 +712,16 @@ __global__ void __launch_bounds__(Geo<T, TX, TY, NS>::NT)
 
       if (live) {
         // receivers in this row segment (velocity after the update, :593-602)
-        if (sample) {
-          int lo = sd.rec_plane[k], hi = sd.rec_plane[k + 1];
-          if (lo < hi) {
+        if (rlo < rhi) {
+          int lo = rlo, hi = rhi;
+          {
+            const int end = hi;
             while (lo < hi) {   // first receiver with (j, i) >= (y, xg)
               const int mid = (lo + hi) >> 1;
               const int4 r = sd.rec_sorted[mid];
               if (r.y < y || (r.y == y && r.x < xg)) lo = mid + 1; else hi = mid;
             }
-            for (int q = lo, qe = sd.rec_plane[k + 1]; q < qe; ++q) {
+            for (int q = lo; q < end; ++q) {
               const int4 r = sd.rec_sorted[q];
               if (r.y != y || r.x >= xg + V) break;
               const int e = r.x - xg;
@@ -675,8 +740,7 @@ __global__ void __launch_bounds__(Geo<T, TX, TY, NS>::NT)
           }
         }
         // force source after the update (cudazerocopy.cu:451-453)
-        if (sd.src_kind == 0 && k == sd.src_k && y == sd.src_j && sd.src_i >= xg && sd.src_i < xg + V &&
-            it_step >= 1 && it_step <= sd.nstep) {
+        if (src_row && k == sd.src_k) {
           const T s = sd.stf[it_step - 1];
           const int se = sd.src_i - xg;
           const bool wx = sd.src_w[0] != T(0), wy = sd.src_w[1] != T(0), wz = sd.src_w[2] != T(0);
@@ -689,35 +753,27 @@ __global__ void __launch_bounds__(Geo<T, TX, TY, NS>::NT)
             vz[c] = (hit && wz) ? vz[c] + fz * dt / rbz[c] : vz[c];
           }
         }
-        const long long g = (long long)k * plane + (long long)y * px + xg;
-        st_vec(sd.f[0] + g, vx);
-        st_vec(sd.f[1] + g, vy);
-        st_vec(sd.f[2] + g, vz);
+        const long long g = (long long)k * plane + rowoff;
+        st_vec(f0 + g, vx);
+        st_vec(f1 + g, vy);
+        st_vec(f2 + g, vz);
         if (in_x) {
-          st_vec(gx + PSI_V0 * sd.psx, px0);
-          st_vec(gx + PSI_V1 * sd.psx, px1);
-          st_vec(gx + PSI_V2 * sd.psx, px2);
+          st_vec(gx + PSI_V0 * psx, px0);
+          st_vec(gx + PSI_V1 * psx, px1);
+          st_vec(gx + PSI_V2 * psx, px2);
         }
         if (in_y) {
-          st_vec(gy + PSI_V0 * sd.psy, py0);
-          st_vec(gy + PSI_V1 * sd.psy, py1);
-          st_vec(gy + PSI_V2 * sd.psy, py2);
+          st_vec(gy + PSI_V0 * psy, py0);
+          st_vec(gy + PSI_V1 * psy, py1);
+          st_vec(gy + PSI_V2 * psy, py2);
         }
         if (in_z) {
-          st_vec(gz + PSI_V0 * sd.psz, pz0);
-          st_vec(gz + PSI_V1 * sd.psz, pz1);
-          st_vec(gz + PSI_V2 * sd.psz, pz2);
+          st_vec(gz + PSI_V0 * psz, pz0);
+          st_vec(gz + PSI_V1 * psz, pz1);
+          st_vec(gz + PSI_V2 * psz, pz2);
         }
       }
-
-      if (__syncthreads_or(timed_out)) {
-        if (tid == 0) atomicOr(err, DEV_ERR_TIMEOUT);
-        for (long long q = consumed; q < pc.n; ++q)
-          mbar_wait_bounded(&full[q % NS], (uint32_t)((q / NS) & 1), 100000000ull);
-        return;
-      }
-      consumed += (k == item.k1 - 1) ? 2 : 1;
-      while (pc.item < pc.end && pc.n < consumed + NS) issue(tid == 0);
+      n += last ? 2 : 1;
     }
   }
 }

@@ -124,6 +124,10 @@ const char *ela3d_last_error(void);
  * cells, sampgat=2, IT_OUTPUT=200, COMPAT profiles, FP32. */
 ela3d_status ela3d_params_default(ela3d_params *p);
 
+/* Makes device `ordinal` current for this thread's later calls (the
+ * reference always uses device 0; one process per GPU selects its own). */
+ela3d_status ela3d_select_device(int32_t ordinal);
+
 /* ---- single shot -------------------------------------------------------- */
 /* Replaces main()'s setup: allocations and zero fill (simpelmodel.cpp:80-140),
  * model fill (:41-59), profile precompute (:142-361).  cp, cs, rho are host
@@ -134,6 +138,9 @@ ela3d_status ela3d_plan_create(const ela3d_params *p, const float *cp, const flo
  * waits for completion; resumable.  Returns ELA3D_ERR_UNSTABLE when the
  * energy monitor trips, ELA3D_ERR_TIMEOUT when a kernel gave up a wait. */
 ela3d_status ela3d_run(ela3d_plan *plan, int32_t nsteps);
+/* ela3d_run bracketed by CUDA events on the plan's stream; *ms receives the
+ * device time of the nsteps steps. */
+ela3d_status ela3d_run_timed(ela3d_plan *plan, int32_t nsteps, double *ms);
 /* Queues nsteps on the plan's stream without waiting. */
 ela3d_status ela3d_enqueue(ela3d_plan *plan, int32_t nsteps);
 /* Waits for queued work and reports device-side errors. */
