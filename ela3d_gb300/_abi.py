@@ -38,8 +38,11 @@ SIGNATURES = [
     ("ela3d_get_kernel_timing", _c.c_int, [_P, _c.POINTER(_c.c_double), _c.POINTER(_c.c_double),
                                            _c.POINTER(_c.c_int64), _c.POINTER(_c.c_int64)]),
     ("ela3d_plan_destroy", _c.c_int, [_P]),
+    ("ela3d_plan_inject_timeout", _c.c_int, [_P, _c.c_int32]),
     ("ela3d_select_device", _c.c_int, [_c.c_int32]),
     ("ela3d_run_timed", _c.c_int, [_P, _c.c_int32, _c.POINTER(_c.c_double)]),
+    ("ela3d_slab_extent", _c.c_int, [_P, _P, _c.c_int32, _c.POINTER(_c.c_int32), _c.POINTER(_c.c_int32)]),
+    ("ela3d_schedule_build", _c.c_int, [_c.c_int32] * 8 + [_c.POINTER(_c.c_int32), _c.POINTER(_c.c_int32), _P, _P]),
     ("ela3d_variant_count", _c.c_int32, []),
     ("ela3d_variant_get", _c.c_int, [_c.c_int32, _P]),
     ("ela3d_plan_create_tuned", _c.c_int, [_c.POINTER(CParams), _P, _P, _P, _P, _c.POINTER(_P)]),
@@ -72,6 +75,29 @@ def variants() -> list[VariantInfo]:
         _check(lib.ela3d_variant_get(i, ctypes.byref(v)), "ela3d_variant_get")
         out.append(v)
     return out
+
+
+def slab_extent(a_full, a_half) -> tuple[int, int]:
+    lib = load_library()
+    a = np.ascontiguousarray(a_full, np.float64)
+    b = np.ascontiguousarray(a_half, np.float64)
+    lo, hi = ctypes.c_int32(), ctypes.c_int32()
+    _check(lib.ela3d_slab_extent(a.ctypes.data, b.ctypes.data, a.size, ctypes.byref(lo), ctypes.byref(hi)),
+           "ela3d_slab_extent")
+    return lo.value, hi.value
+
+
+def schedule(nx, ny, nz, tile_x, tile_y, kind, chunk, max_blocks):
+    """Returns (items [n, 3] of (tile, k0, k1), block_first [nblocks + 1])."""
+    lib = load_library()
+    ni, nb = ctypes.c_int32(), ctypes.c_int32()
+    _check(lib.ela3d_schedule_build(nx, ny, nz, tile_x, tile_y, kind, chunk, max_blocks, ctypes.byref(ni),
+                                    ctypes.byref(nb), None, None), "ela3d_schedule_build")
+    items = np.zeros((ni.value, 3), np.int32)
+    first = np.zeros(nb.value + 1, np.int32)
+    _check(lib.ela3d_schedule_build(nx, ny, nz, tile_x, tile_y, kind, chunk, max_blocks, ctypes.byref(ni),
+                                    ctypes.byref(nb), items.ctypes.data, first.ctypes.data), "ela3d_schedule_build")
+    return items, first
 
 
 class Ela3dError(RuntimeError):
@@ -185,6 +211,11 @@ class Plan:
         _check(self._lib.ela3d_get_kernel_timing(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(na),
                                                  ctypes.byref(nb)), "ela3d_get_kernel_timing")
         return a.value, b.value, na.value, nb.value
+
+    def inject_timeout(self, launches: int) -> None:
+        """Test hook: the next `launches` kernel launches withhold their loads
+        so their bounded waits expire (ELA3D_ERR_TIMEOUT at the next sync)."""
+        _check(self._lib.ela3d_plan_inject_timeout(self._h, launches), "ela3d_plan_inject_timeout")
 
     def close(self) -> None:
         if getattr(self, "_h", None) is not None and self._h.value:

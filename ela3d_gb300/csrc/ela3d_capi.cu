@@ -224,8 +224,48 @@ ela3d_status ela3d_get_kernel_timing(ela3d_plan *plan, double *stress_ms, double
   return plan->eng->timing(stress_ms, velocity_ms, stress_launches, velocity_launches);
 }
 
+ela3d_status ela3d_plan_inject_timeout(ela3d_plan *plan, int32_t launches) {
+  if (!plan) return ELA3D_ERR_INVALID_ARG;
+  return plan->eng->inject_timeout(launches);
+}
+
 ela3d_status ela3d_plan_destroy(ela3d_plan *plan) {
   delete plan;
+  return ELA3D_OK;
+}
+
+ela3d_status ela3d_slab_extent(const double *a_full, const double *a_half, int32_t n, int32_t *lo, int32_t *hi) {
+  if (!a_full || !a_half || n < 1 || !lo || !hi) return ELA3D_ERR_INVALID_ARG;
+  int l = 0, h = 0;
+  slab_extent(a_full, a_half, n, &l, &h);
+  *lo = l;
+  *hi = h;
+  return ELA3D_OK;
+}
+
+ela3d_status ela3d_schedule_build(int32_t nx, int32_t ny, int32_t nz, int32_t tile_x, int32_t tile_y,
+                                  int32_t schedule, int32_t chunk, int32_t max_blocks, int32_t *nitems,
+                                  int32_t *nblocks, int32_t *items, int32_t *block_first) {
+  if (nx < 1 || ny < 1 || nz < 1 || tile_x < 1 || tile_y < 1 || max_blocks < 1 || !nitems || !nblocks)
+    return ELA3D_ERR_INVALID_ARG;
+  std::vector<Item> it;
+  std::vector<int2> rg;
+  build_schedule({ShotShape{nx, ny, nz}}, tile_x, tile_y, schedule, chunk, max_blocks, &it, &rg);
+  if (items) {
+    if (*nitems < (int32_t)it.size()) return ELA3D_ERR_INVALID_ARG;
+    for (size_t q = 0; q < it.size(); ++q) {
+      items[3 * q] = it[q].tile;
+      items[3 * q + 1] = it[q].k0;
+      items[3 * q + 2] = it[q].k1;
+    }
+  }
+  if (block_first) {
+    if (*nblocks < (int32_t)rg.size()) return ELA3D_ERR_INVALID_ARG;
+    for (size_t b = 0; b < rg.size(); ++b) block_first[b] = rg[b].x;
+    block_first[rg.size()] = rg.empty() ? 0 : rg.back().y;
+  }
+  *nitems = (int32_t)it.size();
+  *nblocks = (int32_t)rg.size();
   return ELA3D_OK;
 }
 

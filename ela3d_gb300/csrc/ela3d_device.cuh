@@ -30,6 +30,14 @@ enum : unsigned {
 // Wall-clock limit of one device-side wait (ns).  A wait normally ends in
 // microseconds; the limit only turns a lost transfer into an error status.
 constexpr unsigned long long kWaitLimitNs = 2000000000ull;
+// Limit used when a test asks for the timeout path (20 ms).
+constexpr unsigned long long kTestWaitLimitNs = 20000000ull;
+
+// Kernel control word.  CTL_WITHHOLD_LOADS makes the producer issue no
+// loads, so every consumer wait expires and the kernel returns
+// DEV_ERR_TIMEOUT: the failure path of a lost transfer, exercised without a
+// fault (the waits are bounded, nothing spins forever).
+enum : int { CTL_WITHHOLD_LOADS = 1 };
 
 // Which psi variable of an axis.  Stress half-step: S0..S2, velocity: V0..V2.
 //  x: S0 dvx_dx(half) S1 dvy_dx S2 dvz_dx | V0 dsxx_dx V1 dsxy_dx(half) V2 dsxz_dx(half)

@@ -491,7 +491,9 @@ class Engine final : public EngineBase {
   }
 
   ela3d_status launch_step(int tick) {
-    void *args[] = {&d_desc_, &d_maps_, &d_items_, &d_ranges_, &tick, &d_err_};
+    int ctl = inject_ > 0 ? CTL_WITHHOLD_LOADS : 0;
+    if (inject_ > 0) --inject_;
+    void *args[] = {&d_desc_, &d_maps_, &d_items_, &d_ranges_, &tick, &d_err_, &ctl};
     cudaEvent_t e0 = nullptr, e1 = nullptr, e2 = nullptr;
     if (timing_) {
       e0 = event(); e1 = event(); e2 = event();
@@ -605,6 +607,12 @@ class Engine final : public EngineBase {
     return ELA3D_OK;
   }
 
+  ela3d_status inject_timeout(int launches) override {
+    if (launches < 0) BAD("launches must be >= 0");
+    inject_ = launches;
+    return ELA3D_OK;
+  }
+
   ela3d_status set_timing(bool on) override {
     timing_ = on;
     if (on) { t_stress_ = t_vel_ = 0.0; n_stress_ = n_vel_ = 0; }
@@ -715,6 +723,7 @@ class Engine final : public EngineBase {
   double *d_energy_ = nullptr;
   int nblocks_ = 0;
   int tick_ = 0;
+  int inject_ = 0;   // launches left that withhold their loads (test hook)
   bool timing_ = false;
   std::vector<Ev> pending_;
   std::vector<cudaEvent_t> free_events_;

@@ -63,6 +63,7 @@ class EngineBase {
   virtual ela3d_status energy(int shot, double *out) = 0;
   virtual ela3d_status info(int shot, ela3d_plan_info *out) = 0;
   virtual ela3d_status set_timing(bool on) = 0;
+  virtual ela3d_status inject_timeout(int launches) = 0;
   virtual ela3d_status timing(double *s_ms, double *v_ms, int64_t *ns, int64_t *nv) = 0;
   virtual int nshots() const = 0;
   virtual int steps_done() const = 0;

@@ -97,7 +97,8 @@ __device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
 // nz, which the TMA fills with zeros).
 template <int NS, typename Issue>
 __device__ __forceinline__ void produce(const Item *__restrict__ items, int2 range, uint64_t *full, uint64_t *empty,
-                                        Issue issue, unsigned *__restrict__ err) {
+                                        Issue issue, unsigned *__restrict__ err, int ctl) {
+  if (ctl & CTL_WITHHOLD_LOADS) return;  // test mode: no stage is ever filled
   long long n = 0;
   bool ok = true;
   for (int ii = range.x; ii < range.y && ok; ++ii) {
@@ -122,7 +123,7 @@ template <typename T, int TX, int TY, int NS>
 __global__ void __launch_bounds__(Geo<T, TX, TY, NS>::THREADS, Geo<T, TX, TY, NS>::MINB)
     stress_kernel(const ShotDesc<T> *__restrict__ shots, const ShotMaps *__restrict__ maps,
                   const Item *__restrict__ items, const int2 *__restrict__ ranges, int tick,
-                  unsigned *__restrict__ err) {
+                  unsigned *__restrict__ err, int ctl) {
   using G = Geo<T, TX, TY, NS>;
   constexpr int V = G::VEC, H = G::H, WW = G::WW;
   extern __shared__ __align__(1024) unsigned char smem[];
@@ -159,13 +160,14 @@ __global__ void __launch_bounds__(Geo<T, TX, TY, NS>::THREADS, Geo<T, TX, TY, NS
 #pragma unroll
         for (int c = 0; c < 6; ++c) tma_load_3d(st + G::S_SIG + c * G::SC, &m[6 + c], x0, y0, k, bar);
       };
-      produce<NS>(items, range, full, empty, issue, err);
+      produce<NS>(items, range, full, empty, issue, err, ctl);
     }
     return;
   }
 
   const int lane = tid & 31;
   const int tx = tid % G::NTX, ty = tid / G::NTX;
+  const unsigned long long wait_ns = ctl ? kTestWaitLimitNs : kWaitLimitNs;
   long long n = 0;  // index of the load holding the current plane
 
   for (int ii = range.x; ii < range.y; ++ii) {
@@ -259,8 +261,8 @@ __global__ void __launch_bounds__(Geo<T, TX, TY, NS>::THREADS, Geo<T, TX, TY, NS
       }
 
       const int s0 = (int)(n % NS), s1 = (int)((n + 1) % NS);
-      bool ok = mbar_wait_bounded(&full[s0], (uint32_t)((n / NS) & 1));
-      ok = ok && mbar_wait_bounded(&full[s1], (uint32_t)(((n + 1) / NS) & 1));
+      bool ok = mbar_wait_bounded(&full[s0], (uint32_t)((n / NS) & 1), wait_ns);
+      ok = ok && mbar_wait_bounded(&full[s1], (uint32_t)(((n + 1) / NS) & 1), wait_ns);
       if (__any_sync(0xffffffffu, !ok)) {
         if (lane == 0) atomicOr(err, DEV_ERR_TIMEOUT);
         return;
@@ -436,7 +438,7 @@ template <typename T, int TX, int TY, int NS>
 __global__ void __launch_bounds__(Geo<T, TX, TY, NS>::THREADS, Geo<T, TX, TY, NS>::MINB)
     velocity_kernel(const ShotDesc<T> *__restrict__ shots, const ShotMaps *__restrict__ maps,
                     const Item *__restrict__ items, const int2 *__restrict__ ranges, int tick,
-                    unsigned *__restrict__ err) {
+                    unsigned *__restrict__ err, int ctl) {
   using G = Geo<T, TX, TY, NS>;
   constexpr int V = G::VEC, H = G::H, WW = G::WW;
   extern __shared__ __align__(1024) unsigned char smem[];
@@ -474,13 +476,14 @@ __global__ void __launch_bounds__(Geo<T, TX, TY, NS>::THREADS, Geo<T, TX, TY, NS
 #pragma unroll
         for (int c = 0; c < 3; ++c) tma_load_3d(st + G::V_V + c * G::SC, &m[7 + c], x0, y0, k, bar);
       };
-      produce<NS>(items, range, full, empty, issue, err);
+      produce<NS>(items, range, full, empty, issue, err, ctl);
     }
     return;
   }
 
   const int lane = tid & 31;
   const int tx = tid % G::NTX, ty = tid / G::NTX;
+  const unsigned long long wait_ns = ctl ? kTestWaitLimitNs : kWaitLimitNs;
   constexpr int CS = G::SC / (int)sizeof(T);
   long long n = 0;
 
@@ -588,8 +591,8 @@ __global__ void __launch_bounds__(Geo<T, TX, TY, NS>::THREADS, Geo<T, TX, TY, NS
       }
 
       const int s0 = (int)(n % NS), s1 = (int)((n + 1) % NS);
-      bool ok = mbar_wait_bounded(&full[s0], (uint32_t)((n / NS) & 1));
-      ok = ok && mbar_wait_bounded(&full[s1], (uint32_t)(((n + 1) / NS) & 1));
+      bool ok = mbar_wait_bounded(&full[s0], (uint32_t)((n / NS) & 1), wait_ns);
+      ok = ok && mbar_wait_bounded(&full[s1], (uint32_t)(((n + 1) / NS) & 1), wait_ns);
       if (__any_sync(0xffffffffu, !ok)) {
         if (lane == 0) atomicOr(err, DEV_ERR_TIMEOUT);
         return;

@@ -163,6 +163,12 @@ ela3d_status ela3d_set_kernel_timing(ela3d_plan *plan, int32_t enable);
 ela3d_status ela3d_get_kernel_timing(ela3d_plan *plan, double *stress_ms, double *velocity_ms,
                                      int64_t *stress_launches, int64_t *velocity_launches);
 ela3d_status ela3d_plan_destroy(ela3d_plan *plan);
+/* Test hook for the failure path: the kernels of the plan's next `steps`
+ * time steps withhold their shared-memory loads, so their bounded device
+ * waits expire (20 ms) and the next ela3d_sync/ela3d_run reports
+ * ELA3D_ERR_TIMEOUT.  Nothing faults or hangs; the CUDA context stays usable,
+ * the plan's fields are left partly updated.  No reference counterpart. */
+ela3d_status ela3d_plan_inject_timeout(ela3d_plan *plan, int32_t steps);
 
 /* ---- kernel variants and tuning ----------------------------------------- */
 /* A compiled instance of the stress/velocity kernel pair: real type, x-y
@@ -188,6 +194,22 @@ ela3d_status ela3d_variant_get(int32_t index, ela3d_variant_info *out);
 /* ela3d_plan_create with an explicit kernel variant and schedule. */
 ela3d_status ela3d_plan_create_tuned(const ela3d_params *p, const float *cp, const float *cs,
                                      const float *rho, const ela3d_tuning *tune, ela3d_plan **out);
+
+/* ---- host-side planning (no GPU needed) ---------------------------------- */
+/* C-PML slab extent of one axis from its 'a' profiles: cells [0, lo) and
+ * [hi, n) may carry memory variables; every cell of [lo, hi) has a = 0 in
+ * both the full- and half-node profile, so its memory variables stay 0 and
+ * are not stored (the reference stores all 18 for every cell,
+ * simpelmodel.cpp:89-106).  lo == hi == n when the layer covers the axis. */
+ela3d_status ela3d_slab_extent(const double *a_full, const double *a_half, int32_t n,
+                               int32_t *lo, int32_t *hi);
+/* The work split the kernels use for one grid: items (tile, k0, k1) per
+ * block.  With items == NULL only the counts are returned.  No reference
+ * counterpart (its launch is a fixed 3-D grid, cudazerocopy.cu:1361-1369). */
+ela3d_status ela3d_schedule_build(int32_t nx, int32_t ny, int32_t nz, int32_t tile_x, int32_t tile_y,
+                                  int32_t schedule, int32_t chunk, int32_t max_blocks,
+                                  int32_t *nitems, int32_t *nblocks,
+                                  int32_t *items /* nitems x 3 */, int32_t *block_first /* nblocks+1 */);
 
 #ifdef __cplusplus
 }

@@ -22,9 +22,9 @@ times so that a different reference fails loudly:
 - per-step console output is removed;
 - receivers are recorded from the velocity after the update, before the
   source, exactly where the program gathers its plane (:592-604);
-- optional "clean" switch fixes the a_x_half assignment (:223) and the zmin
-  half-node abscissa (:331) and per-axis z normalisation, for checking the
-  textbook C-PML variant;
+- optional "clean" switch fixes the a_x_half assignment (:223), the zmin
+  half-node abscissa (:331) and the z normalisation, and clamps alpha at 0 on
+  y and z as on x (:217-218), for checking the textbook C-PML variant;
 - a float64 variant replaces ``float`` by ``double`` and the f-suffixed
   libm calls by their double versions.
 
@@ -94,7 +94,13 @@ def patch(src: str) -> str:
     zsec = _sub(zsec, "abscissa_normalized = abscissa_in_PML / thickness_PML_y;",
                 "abscissa_normalized = abscissa_in_PML / (g_cfg.clean ? thickness_PML_z : thickness_PML_y);",
                 count=3)
+    zsec = _sub(zsec, "\t\tcb_z[i] = expf(",
+                "\t\tif (g_cfg.clean) { if (calpha_z[i] < 0.0) calpha_z[i] = 0.0;"
+                " if (calpha_z_half[i] < 0.0) calpha_z_half[i] = 0.0; }\n\t\tcb_z[i] = expf(")
     s = head + "//-----------------PML Z" + zsec + "float *gatvx" + tail
+    s = _sub(s, "\t\tcb_y[i] = expf(",
+             "\t\tif (g_cfg.clean) { if (calpha_y[i] < 0.0) calpha_y[i] = 0.0;"
+             " if (calpha_y_half[i] < 0.0) calpha_y_half[i] = 0.0; }\n\t\tcb_y[i] = expf(")
     # time loop hooks
     s = _sub(s, "for (int it = 1; it <= NSTEP; it++) {",
              "for (int it = 1; it <= NSTEP; it++) {\n\t\tref_step_hook(it);")

@@ -1,0 +1,118 @@
+"""GPU results against the reference program's own outputs and at full size.
+
+- tests/golden: fixtures written by the reference CPU program
+  (seismicCPML_3d_isotropic_simpelmodel.cpp); FP32 GPU within 2e-5 relative
+  L2, FP64 GPU within 1e-11.
+- Full-size accuracy of the production FP32 path against the FP64 build of
+  the same kernels: every seismogram within 1e-4 relative L2 (the target),
+  with the final wavefield's error reported.
+- Symmetry of a centred source in a homogeneous cube (full-size indexing).
+"""
+import glob
+import os
+import sys
+
+import numpy as np
+import pytest
+
+from conftest import rel_l2
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(HERE, "golden"))
+import make_golden  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+GOLD = sorted(glob.glob(os.path.join(HERE, "golden", "ref_*.npz")))
+CASES = make_golden.cases()
+
+
+def run(p, cp, cs, rho, **kw):
+    from ela3d_gb300 import Plan
+
+    with Plan(p, cp, cs, rho, **kw) as plan:
+        plan.run(p.nstep)
+        fp64 = p.precision == 1
+        return plan.seismograms(fp64=fp64), np.stack([plan.field(c, fp64=fp64) for c in range(9)])
+
+
+@pytest.mark.parametrize("path", GOLD, ids=[os.path.basename(g)[4:-4] for g in GOLD])
+def test_gpu_matches_reference_program_goldens(built, path):
+    name = os.path.basename(path)[4:-4]
+    p, cp, cs, rho = CASES[name]
+    g = np.load(path)
+    for tag, prec, tol in (("f32", 0, 2e-5), ("f64", 1, 1e-11)):
+        if f"seis_{tag}" not in g:
+            continue
+        seis, fields = run(p.with_(precision=prec), cp, cs, rho)
+        assert rel_l2(seis, g[f"seis_{tag}"]) <= tol, (name, tag, rel_l2(seis, g[f"seis_{tag}"]))
+        s = make_golden.summarize(p, fields)
+        slice_tol = 5 * tol   # single slices of nearly silent components
+        for c in range(9):
+            for key in ("slice_xy", "slice_yz"):
+                want = g[f"{key}_{tag}"][c]
+                if np.any(want):
+                    assert rel_l2(s[key][c], want) <= slice_tol, (name, tag, key, c)
+        assert np.allclose(s["sumsq"], g[f"sumsq_{tag}"], rtol=10 * tol, atol=0)
+
+
+def seismogram_errors(s, ref):
+    """Relative L2 error of every seismogram (one receiver's vx, vy, vz
+    record) and of the whole set."""
+    per_rec = [rel_l2(s[r], ref[r]) for r in range(s.shape[0]) if np.any(ref[r])]
+    return per_rec, rel_l2(s, ref)
+
+
+def _fp32_vs_fp64(p, cp, cs, rho):
+    s32, f32 = run(p, cp, cs, rho)
+    s64, f64 = run(p.with_(precision=1), cp, cs, rho)
+    per_rec, whole = seismogram_errors(s32.astype(np.float64), s64)
+    wave = [rel_l2(f32[c], f64[c]) for c in range(9)]
+    return per_rec, whole, wave, s32, s64
+
+
+def test_homogeneous_101_fp32_vs_fp64(built):
+    """101^3 cube, 1000 steps: every seismogram within 1e-4 of FP64, and the
+    FP32 path no less accurate than the reference program's own FP32."""
+    import oracle
+    from ela3d_gb300 import configs
+
+    p, cp, cs, rho = configs.homogeneous_101()
+    per_rec, whole, wave, s32, s64 = _fp32_vs_fp64(p, cp, cs, rho)
+    ref32, _ = oracle.run(p, cp, cs, rho, want_fields=False)
+    ref_rec, ref_whole = seismogram_errors(ref32.astype(np.float64), s64)
+    print(f"homogeneous_101: worst seismogram rel L2 {max(per_rec):.2e} (reference FP32 {max(ref_rec):.2e}), "
+          f"all {whole:.2e} (reference FP32 {ref_whole:.2e}), final wavefield {max(wave):.2e}")
+    assert max(per_rec) <= 1e-4 and whole <= 1e-4
+    assert max(per_rec) <= max(ref_rec) and whole <= ref_whole
+    assert max(wave) <= 1e-3
+    assert rel_l2(s32, ref32) <= 1e-4
+
+
+def test_anticline_256_fp32_vs_fp64(built):
+    """256^3 anticline, 2000 steps: every seismogram within 1e-4 of FP64."""
+    from ela3d_gb300 import configs
+
+    p, cp, cs, rho = configs.anticline_256()
+    per_rec, whole, wave, _, _ = _fp32_vs_fp64(p, cp, cs, rho)
+    print(f"anticline_256: worst seismogram rel L2 {max(per_rec):.2e}, all {whole:.2e}, "
+          f"final wavefield {max(wave):.2e}")
+    assert max(per_rec) <= 1e-4 and whole <= 1e-4
+    assert max(wave) <= 1e-3
+
+
+def test_centred_source_symmetry(built):
+    """vz from a vertical force at the centre of a homogeneous cube with the
+    clean profiles is mirror-symmetric in x and y about the source (the
+    staggering makes vz a cell-centred quantity in x and y)."""
+    from ela3d_gb300 import PML_CLEAN, Plan, ShotParams, media
+
+    n = 129
+    p = ShotParams(nx=n, ny=n, nz=n, nstep=150, dt=1e-3, npml=12, pml_mode=PML_CLEAN, f0=15.0, t0=1.2 / 15.0,
+                   src=(64, 64, 64))
+    cp, cs, rho = media.homogeneous(n, n, n, 3000.0, 1700.0, 2200.0)
+    with Plan(p, cp, cs, rho) as plan:
+        plan.run(p.nstep)
+        vz = plan.field(2).astype(np.float64)
+    core = vz[1:-1, 1:-1, 1:-1]
+    assert rel_l2(core, core[:, :, ::-1]) < 1e-5
+    assert rel_l2(core, core[:, ::-1, :]) < 1e-5
