@@ -16,6 +16,9 @@ over ranks.  Also reported:
             read-back), wall clock;
   cpu_baseline  the reference CPU program (oracle/_ref, else the oracle's C
             restatement) on 1 core, a bounded sample of the same shot.
+Also in the same line: "batched" (64 shots of the 256^3 anticline sharing
+one model, advanced together) and "uneven" (48 uneven grids together vs one
+at a time), each next to the single-shot path on the same GPU.
 Reference arm (--impl reference): the reference CPU program itself on all
 host cores (one process per core, each a bounded sample of the same shot),
 rank 0 only.
@@ -314,6 +317,11 @@ def run_ours(args, rank, world, local):
             "kernels": kern}
     roof["step_frac"] = roof["step_achieved_gbs"] / peak
 
+    extra = {}
+    if not args.no_batched:
+        extra["batched"] = batched_shots(args, value)
+        extra["uneven"] = uneven_batch(args)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         try:
@@ -329,7 +337,67 @@ def run_ours(args, rank, world, local):
                 "config": config_block(p, {"steps_timed": args.steps}),
                 "e2e": e2e, "gpu_launches": int(2 * args.steps * world), "roofline": roof,
                 "cpu_baseline": cpu, "clocks": clk}
+        line.update(extra)
         print(json.dumps(line), flush=True)
+
+
+def batched_shots(args, single_value: float) -> dict:
+    """64 shots of the 256^3 anticline (8 x 8 source grid at z = npml + 3,
+    one shared model) advanced together; graph replay, CUDA-event timing."""
+    import ela3d_gb300 as E
+    from ela3d_gb300 import configs
+    from ela3d_gb300.metrics import bytes_per_cell
+
+    shots, cp, cs, rho = configs.anticline_256_shots(args.batch_shots)
+    cells = sum(p.cells for p in shots)
+    t0 = time.perf_counter()
+    with E.Batch([(p, cp, cs, rho) for p in shots], schedule=args.batch_schedule, chunk=args.batch_chunk) as b:
+        t_create = time.perf_counter() - t0
+        b.run(args.warmup)
+        ms = b.run_timed(args.batch_steps)
+        t1 = time.perf_counter()
+        b.run(0)
+        seis = [b.seismograms(q) for q in range(len(shots))]
+        t_read = time.perf_counter() - t1
+    value = cells * args.batch_steps / (ms / 1e3) / 1e9
+    bpc = bytes_per_cell(256, 256, 256, 16)["step"]
+    peak, _ = measured_peaks()
+    return {"workload": f"anticline_256_shots: {len(shots)} shots of 256^3 sharing one model, FP32, "
+                        f"8x8 source grid at z=19, 201-receiver line each",
+            "metric": METRIC, "value": value, "steps_timed": args.batch_steps,
+            "ms_per_step": ms / args.batch_steps, "single_shot_value": single_value,
+            "ratio_vs_single_shot": value / single_value,
+            "frac_of_hbm_at_142B": value * bpc / peak,
+            "create_s": t_create, "readback_s": t_read,
+            "schedule": {"kind": args.batch_schedule, "chunk": args.batch_chunk},
+            "timing": "CUDA events around replayed 50-step graphs; model stored once"}
+
+
+def uneven_batch(args) -> dict:
+    """48 grids with edges from multiples of 16 in [64, 320] (seed 1): all
+    together vs the same instances one at a time (each alone on the GPU)."""
+    import ela3d_gb300 as E
+    from ela3d_gb300 import configs
+
+    inst = configs.uneven_batch(count=args.uneven_count)
+    steps = args.uneven_steps
+    cells = sum(p.cells for p, *_ in inst)
+    alone_s = 0.0
+    for p, cp, cs, rho in inst:
+        with E.Plan(p, cp, cs, rho) as pl:
+            pl.run(3)
+            alone_s += pl.run_timed(steps) / 1e3
+    alone = cells * steps / alone_s / 1e9
+    with E.Batch(inst) as b:
+        b.run(3)
+        ms = b.run_timed(steps)
+    value = cells * steps / (ms / 1e3) / 1e9
+    sizes = [p.cells for p, *_ in inst]
+    return {"workload": f"uneven_batch: {len(inst)} grids, edges from multiples of 16 in [64, 320] (seed 1), "
+                        f"{min(sizes) / 1e6:.2f}-{max(sizes) / 1e6:.1f} Mcells, random 3-6 layer domes, FP32",
+            "metric": METRIC, "value": value, "steps_timed": steps,
+            "single_shot_sequential_value": alone, "ratio_vs_single_shot": value / alone,
+            "timing": "CUDA events; the same steps of every instance, batched vs one plan at a time"}
 
 
 def run_reference(args, rank, world, local):
@@ -356,6 +424,13 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end shot (short profiling runs)")
+    ap.add_argument("--no-batched", action="store_true", help="skip the batched and uneven workloads")
+    ap.add_argument("--batch-shots", type=int, default=64)
+    ap.add_argument("--batch-steps", type=int, default=100)
+    ap.add_argument("--batch-schedule", type=int, default=2)
+    ap.add_argument("--batch-chunk", type=int, default=16)
+    ap.add_argument("--uneven-count", type=int, default=48)
+    ap.add_argument("--uneven-steps", type=int, default=100)
     ap.add_argument("--cpu-steps", type=int, default=20)
     ap.add_argument("--ref-steps-cap", type=int, default=20)
     args = ap.parse_args()

@@ -43,6 +43,13 @@ SIGNATURES = [
     ("ela3d_run_timed", _c.c_int, [_P, _c.c_int32, _c.POINTER(_c.c_double)]),
     ("ela3d_slab_extent", _c.c_int, [_P, _P, _c.c_int32, _c.POINTER(_c.c_int32), _c.POINTER(_c.c_int32)]),
     ("ela3d_schedule_build", _c.c_int, [_c.c_int32] * 8 + [_c.POINTER(_c.c_int32), _c.POINTER(_c.c_int32), _P, _P]),
+    ("ela3d_batch_create", _c.c_int, [_c.c_int32, _P, _P, _P, _P, _P, _c.POINTER(_P)]),
+    ("ela3d_batch_run", _c.c_int, [_P, _c.c_int32]),
+    ("ela3d_batch_run_timed", _c.c_int, [_P, _c.c_int32, _c.POINTER(_c.c_double)]),
+    ("ela3d_batch_get_seismograms", _c.c_int, [_P, _c.c_int32, _P]),
+    ("ela3d_batch_get_field", _c.c_int, [_P, _c.c_int32, _c.c_int32, _P]),
+    ("ela3d_batch_info", _c.c_int, [_P, _c.c_int32, _P]),
+    ("ela3d_batch_destroy", _c.c_int, [_P]),
     ("ela3d_variant_count", _c.c_int32, []),
     ("ela3d_variant_get", _c.c_int, [_c.c_int32, _P]),
     ("ela3d_plan_create_tuned", _c.c_int, [_c.POINTER(CParams), _P, _P, _P, _P, _c.POINTER(_P)]),
@@ -237,3 +244,80 @@ class Plan:
 
 def is_fp64(p: ShotParams) -> bool:
     return p.precision == FP64
+
+
+class Batch:
+    """Many shots advanced together (ela3d_batch_*).  `shots` is a list of
+    (ShotParams, cp, cs, rho); passing the same model arrays for several
+    shots stores that model once on the device."""
+
+    def __init__(self, shots, variant: int = -1, schedule: int = -1, chunk: int = 0, blocks_per_sm: int = -1):
+        lib = load_library()
+        self._lib = lib
+        self.params = [s[0] for s in shots]
+        n = len(shots)
+        structs = (CParams * n)()
+        keep = []
+        ptrs = {k: (ctypes.c_void_p * n)() for k in ("cp", "cs", "rho")}
+        seen = {}
+        for i, (p, cp, cs, rho) in enumerate(shots):
+            c, rec = p.to_c()
+            structs[i] = c
+            keep.append(rec)
+            for key, arr in (("cp", cp), ("cs", cs), ("rho", rho)):
+                m = seen.get(id(arr))
+                if m is None:
+                    m = np.ascontiguousarray(arr, dtype=np.float32).reshape(-1)
+                    if m.size != p.cells:
+                        raise ValueError("model arrays must hold nx*ny*nz float32 values")
+                    seen[id(arr)] = m
+                    keep.append(m)
+                ptrs[key][i] = m.ctypes.data
+        t = Tuning(variant, schedule, chunk, blocks_per_sm)
+        h = ctypes.c_void_p()
+        _check(lib.ela3d_batch_create(n, structs, ptrs["cp"], ptrs["cs"], ptrs["rho"], ctypes.byref(t),
+                                      ctypes.byref(h)), "ela3d_batch_create")
+        self._h = h
+
+    def run(self, nsteps: int) -> None:
+        _check(self._lib.ela3d_batch_run(self._h, nsteps), "ela3d_batch_run")
+
+    def run_timed(self, nsteps: int) -> float:
+        ms = ctypes.c_double()
+        _check(self._lib.ela3d_batch_run_timed(self._h, nsteps, ctypes.byref(ms)), "ela3d_batch_run_timed")
+        return ms.value
+
+    def seismograms(self, shot: int) -> np.ndarray:
+        p = self.params[shot]
+        out = np.zeros((p.nrec, 3, p.nsamp), np.float32)
+        if out.size:
+            _check(self._lib.ela3d_batch_get_seismograms(self._h, shot, _ptr(out)), "ela3d_batch_get_seismograms")
+        return out
+
+    def field(self, shot: int, comp: int) -> np.ndarray:
+        p = self.params[shot]
+        out = np.empty((p.nz, p.ny, p.nx), np.float32)
+        _check(self._lib.ela3d_batch_get_field(self._h, shot, comp, _ptr(out)), "ela3d_batch_get_field")
+        return out
+
+    def info(self, shot: int) -> PlanInfo:
+        i = PlanInfo()
+        _check(self._lib.ela3d_batch_info(self._h, shot, ctypes.byref(i)), "ela3d_batch_info")
+        return i
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) is not None and self._h.value:
+            self._lib.ela3d_batch_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -95,9 +95,10 @@ __global__ void pad_kernel(const float *__restrict__ src, T *__restrict__ dst, i
 // Explosive source after the velocity half-step, simpelmodel.cpp:607-622:
 // sigma_nn += w_nn s dt (lambda + 2 mu) with (w) = (sin a, sin a, cos a).
 template <typename T>
-__global__ void explosive_kernel(const ShotDesc<T> *shots, int nshots, int tick) {
+__global__ void explosive_kernel(const ShotDesc<T> *shots, int nshots, int tick, const int *dtick) {
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= nshots) return;
+  if (dtick) tick += *dtick;
   const ShotDesc<T> &sd = shots[q];
   if (sd.src_kind != 1) return;
   const int it = tick - sd.tick0;
@@ -151,6 +152,19 @@ __global__ void energy_kernel(const ShotDesc<T> *shot, int nx, int ny, int nz, d
   }
 }
 
+// Device step counter for replayable CUDA graphs.
+__global__ void tick_set_kernel(int *dtick, int value) { *dtick = value; }
+__global__ void tick_add_kernel(int *dtick, int delta) { *dtick += delta; }
+
+cudaError_t launch_tick_set(int *dtick, int value, cudaStream_t s) {
+  tick_set_kernel<<<1, 1, 0, s>>>(dtick, value);
+  return cudaGetLastError();
+}
+cudaError_t launch_tick_add(int *dtick, int delta, cudaStream_t s) {
+  tick_add_kernel<<<1, 1, 0, s>>>(dtick, delta);
+  return cudaGetLastError();
+}
+
 static int blocks_for(long long n, int threads, int cap) {
   long long b = (n + threads - 1) / threads;
   if (b > cap) b = cap;
@@ -181,12 +195,14 @@ cudaError_t launch_pad_f64(const float *src, double *dst, int nx, int ny, int nz
   pad_kernel<double><<<blocks_for((long long)px * ny * nz, 256, 4096), 256, 0, s>>>(src, dst, nx, ny, nz, px);
   return cudaGetLastError();
 }
-cudaError_t launch_explosive_f32(const ShotDesc<float> *shots, int nshots, int tick, cudaStream_t s) {
-  explosive_kernel<float><<<(nshots + 63) / 64, 64, 0, s>>>(shots, nshots, tick);
+cudaError_t launch_explosive_f32(const ShotDesc<float> *shots, int nshots, int tick, const int *dtick,
+                                 cudaStream_t s) {
+  explosive_kernel<float><<<(nshots + 63) / 64, 64, 0, s>>>(shots, nshots, tick, dtick);
   return cudaGetLastError();
 }
-cudaError_t launch_explosive_f64(const ShotDesc<double> *shots, int nshots, int tick, cudaStream_t s) {
-  explosive_kernel<double><<<(nshots + 63) / 64, 64, 0, s>>>(shots, nshots, tick);
+cudaError_t launch_explosive_f64(const ShotDesc<double> *shots, int nshots, int tick, const int *dtick,
+                                 cudaStream_t s) {
+  explosive_kernel<double><<<(nshots + 63) / 64, 64, 0, s>>>(shots, nshots, tick, dtick);
   return cudaGetLastError();
 }
 cudaError_t launch_energy_f32(const ShotDesc<float> *shot, int nx, int ny, int nz, double *out, cudaStream_t s) {

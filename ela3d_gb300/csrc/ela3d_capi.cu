@@ -12,6 +12,11 @@ struct ela3d_plan {
   ela3d_params p{};
 };
 
+struct ela3d_batch {
+  std::unique_ptr<EngineBase> eng;
+  int fp64 = 0;
+};
+
 extern "C" {
 
 const char *ela3d_version(void) { return "ela3d-gb300 0.1"; }
@@ -266,6 +271,84 @@ ela3d_status ela3d_schedule_build(int32_t nx, int32_t ny, int32_t nz, int32_t ti
   }
   *nitems = (int32_t)it.size();
   *nblocks = (int32_t)rg.size();
+  return ELA3D_OK;
+}
+
+ela3d_status ela3d_batch_create(int32_t nshots, const ela3d_params *params, const float *const *cp,
+                                const float *const *cs, const float *const *rho, const ela3d_tuning *tune,
+                                ela3d_batch **out) {
+  if (!out || nshots < 1 || !params || !cp || !cs || !rho) return ELA3D_ERR_INVALID_ARG;
+  *out = nullptr;
+  for (int i = 0; i < nshots; ++i) {
+    ela3d_status st = validate_params(params[i]);
+    if (st != ELA3D_OK) {
+      set_last_error("shot " + std::to_string(i) + ": " + last_error());
+      return st;
+    }
+    if (params[i].precision != params[0].precision) {
+      set_last_error("all shots of a batch need the same precision");
+      return ELA3D_ERR_INVALID_ARG;
+    }
+    if (!cp[i] || !cs[i] || !rho[i]) {
+      set_last_error("model arrays missing");
+      return ELA3D_ERR_INVALID_ARG;
+    }
+  }
+  ela3d_batch *b = new (std::nothrow) ela3d_batch();
+  if (!b) return ELA3D_ERR_OOM;
+  b->fp64 = params[0].precision == ELA3D_FP64;
+  ela3d_status st;
+  b->eng = make_engine(b->fp64, &st);
+  for (int i = 0; i < nshots && st == ELA3D_OK; ++i) {
+    int share = -1;
+    for (int j = 0; j < i && share < 0; ++j)
+      if (cp[j] == cp[i] && cs[j] == cs[i] && rho[j] == rho[i] && params[j].nx == params[i].nx &&
+          params[j].ny == params[i].ny && params[j].nz == params[i].nz)
+        share = j;
+    st = b->eng->add_shot(params[i], cp[i], cs[i], rho[i], share);
+  }
+  if (st == ELA3D_OK) {
+    b->eng->set_retire(true);
+    const TuneChoice c = resolve_tuning(params[0], tune);
+    st = b->eng->finalize(&c);
+  }
+  if (st != ELA3D_OK) {
+    delete b;
+    return st;
+  }
+  *out = b;
+  return ELA3D_OK;
+}
+
+ela3d_status ela3d_batch_run(ela3d_batch *b, int32_t nsteps) {
+  if (!b || nsteps < 0) return ELA3D_ERR_INVALID_ARG;
+  ela3d_status st = b->eng->enqueue(nsteps);
+  if (st != ELA3D_OK) return st;
+  return b->eng->sync();
+}
+
+ela3d_status ela3d_batch_run_timed(ela3d_batch *b, int32_t nsteps, double *ms) {
+  if (!b || nsteps < 0) return ELA3D_ERR_INVALID_ARG;
+  return b->eng->run_timed(nsteps, ms);
+}
+
+ela3d_status ela3d_batch_get_seismograms(ela3d_batch *b, int32_t shot, float *out) {
+  if (!b || !out) return ELA3D_ERR_INVALID_ARG;
+  return b->eng->seismograms(shot, out, 0);
+}
+
+ela3d_status ela3d_batch_get_field(ela3d_batch *b, int32_t shot, int32_t comp, float *out) {
+  if (!b || !out) return ELA3D_ERR_INVALID_ARG;
+  return b->eng->field(shot, comp, out, 0);
+}
+
+ela3d_status ela3d_batch_info(ela3d_batch *b, int32_t shot, ela3d_plan_info *out) {
+  if (!b || !out) return ELA3D_ERR_INVALID_ARG;
+  return b->eng->info(shot, out);
+}
+
+ela3d_status ela3d_batch_destroy(ela3d_batch *b) {
+  delete b;
   return ELA3D_OK;
 }
 

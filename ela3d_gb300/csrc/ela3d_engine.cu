@@ -79,12 +79,13 @@ void build_schedule(const std::vector<ShotShape> &shots, int tx, int ty, int kin
                     std::vector<Item> *items, std::vector<int2> *ranges) {
   items->clear();
   ranges->clear();
+  auto sid = [&](int s) { return shots[s].id >= 0 ? shots[s].id : s; };
   struct Col { int shot, tile, nz; };
   std::vector<Col> cols;
   long long units = 0;
   for (int s = 0; s < (int)shots.size(); ++s) {
     const int ntiles = ((shots[s].nx + tx - 1) / tx) * ((shots[s].ny + ty - 1) / ty);
-    for (int t = 0; t < ntiles; ++t) cols.push_back({s, t, shots[s].nz});
+    for (int t = 0; t < ntiles; ++t) cols.push_back({sid(s), t, shots[s].nz});
     units += (long long)ntiles * shots[s].nz;
   }
   if (units == 0 || max_blocks < 1) return;
@@ -107,14 +108,22 @@ void build_schedule(const std::vector<ShotShape> &shots, int tx, int ty, int kin
     }
     return;
   }
-  // kind 1: z-chunks dealt round-robin in (shot, chunk, tile) order
+  // kinds 1 and 2: z-chunks dealt round-robin.  Kind 1 orders them
+  // (shot, chunk, tile); kind 2 orders (chunk, tile, shot), so blocks running
+  // together hold the same tile of different shots (a shared model tile is
+  // then read from L2 by all but the first).
   if (chunk < 1) chunk = 1;
   std::vector<Item> all;
   for (int s = 0; s < (int)shots.size(); ++s) {
     const int ntiles = ((shots[s].nx + tx - 1) / tx) * ((shots[s].ny + ty - 1) / ty);
     for (int k0 = 0; k0 < shots[s].nz; k0 += chunk)
-      for (int t = 0; t < ntiles; ++t) all.push_back({s, t, k0, std::min(k0 + chunk, shots[s].nz)});
+      for (int t = 0; t < ntiles; ++t) all.push_back({sid(s), t, k0, std::min(k0 + chunk, shots[s].nz)});
   }
+  if (kind == 2)
+    std::stable_sort(all.begin(), all.end(), [](const Item &a, const Item &b) {
+      if (a.k0 != b.k0) return a.k0 < b.k0;
+      return a.tile < b.tile;
+    });
   const int G = (int)std::min<long long>(max_blocks, (long long)all.size());
   for (int b = 0; b < G; ++b) {
     const int first = (int)items->size();
@@ -194,8 +203,8 @@ template <> struct Fp<float> {
   static cudaError_t pad(const float *src, float *dst, int nx, int ny, int nz, int px, cudaStream_t s) {
     return launch_pad_f32(src, dst, nx, ny, nz, px, s);
   }
-  static cudaError_t explosive(const ShotDesc<float> *d, int n, int tick, cudaStream_t s) {
-    return launch_explosive_f32(d, n, tick, s);
+  static cudaError_t explosive(const ShotDesc<float> *d, int n, int tick, const int *dt, cudaStream_t s) {
+    return launch_explosive_f32(d, n, tick, dt, s);
   }
   static cudaError_t energy(const ShotDesc<float> *d, int nx, int ny, int nz, double *o, cudaStream_t s) {
     return launch_energy_f32(d, nx, ny, nz, o, s);
@@ -207,8 +216,8 @@ template <> struct Fp<double> {
   static cudaError_t pad(const float *src, double *dst, int nx, int ny, int nz, int px, cudaStream_t s) {
     return launch_pad_f64(src, dst, nx, ny, nz, px, s);
   }
-  static cudaError_t explosive(const ShotDesc<double> *d, int n, int tick, cudaStream_t s) {
-    return launch_explosive_f64(d, n, tick, s);
+  static cudaError_t explosive(const ShotDesc<double> *d, int n, int tick, const int *dt, cudaStream_t s) {
+    return launch_explosive_f64(d, n, tick, dt, s);
   }
   static cudaError_t energy(const ShotDesc<double> *d, int nx, int ny, int nz, double *o, cudaStream_t s) {
     return launch_energy_f64(d, nx, ny, nz, o, s);
@@ -230,6 +239,8 @@ class Engine final : public EngineBase {
     CK(cudaMalloc(&d_err_, sizeof(unsigned)));
     CK(cudaMemset(d_err_, 0, sizeof(unsigned)));
     CK(cudaMalloc(&d_energy_, sizeof(double)));
+    CK(cudaMalloc(&d_tick_, sizeof(int)));
+    CK(cudaMemset(d_tick_, 0, sizeof(int)));
     return ELA3D_OK;
   }
 
@@ -431,93 +442,215 @@ class Engine final : public EngineBase {
     if (c.variant < 0 || c.variant >= nv || vs[c.variant].fp64 != (sizeof(T) == 8)) BAD("bad kernel variant");
     var_ = &vs[c.variant];
     choice_ = c;
-    const int TX = var_->tx, TY = var_->ty, H = var_->halo;
-    std::vector<ShotShape> shapes;
     for (auto &sp : shots_) {
-      Shot<T> &s = *sp;
-      ShotDesc<T> &d = s.d;
-      const int nx = d.nx, ny = d.ny, nz = d.nz, px = d.px;
-      CUtensorMap *m = s.maps.stress;
-      ela3d_status st;
-#define ENC(map, ptr, bw, bh) \
-  if ((st = encode_map<T>(map, ptr, nx, ny, nz, px, bw, bh)) != ELA3D_OK) return st
-      ENC(&m[0], d.f[0], TX + H, TY + 1);
-      ENC(&m[1], d.f[1], TX + H, TY + 1);
-      ENC(&m[2], d.f[2], TX + H, TY + 1);
-      ENC(&m[3], d.cs, TX + H, TY + 1);
-      ENC(&m[4], d.rho, TX + H, TY + 1);
-      ENC(&m[5], d.cp, TX, TY);
-      for (int q = 0; q < 6; ++q) ENC(&m[6 + q], d.f[3 + q], TX, TY);
-      CUtensorMap *v = s.maps.vel;
-      ENC(&v[0], d.f[3], TX + H, TY);      // sxx
-      ENC(&v[1], d.f[4], TX, TY + 1);      // syy
-      ENC(&v[2], d.f[5], TX, TY);          // szz
-      ENC(&v[3], d.f[6], TX + H, TY + 1);  // sxy
-      ENC(&v[4], d.f[7], TX + H, TY);      // sxz
-      ENC(&v[5], d.f[8], TX, TY + 1);      // syz
-      ENC(&v[6], d.rho, TX + H, TY + 1);   // rho
-      for (int q = 0; q < 3; ++q) ENC(&v[7 + q], d.f[q], TX, TY);
-#undef ENC
-      shapes.push_back({nx, ny, nz});
+      ela3d_status st = encode_shot_maps(*sp);
+      if (st != ELA3D_OK) return st;
     }
     CK(cudaFuncSetAttribute(var_->stress, cudaFuncAttributeMaxDynamicSharedMemorySize, var_->stress_smem));
     CK(cudaFuncSetAttribute(var_->velocity, cudaFuncAttributeMaxDynamicSharedMemorySize, var_->vel_smem));
     int occ_s = 0, occ_v = 0;
     CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_s, var_->stress, var_->threads, var_->stress_smem));
     CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_v, var_->velocity, var_->threads, var_->vel_smem));
-    int per_sm = std::max(1, std::min(occ_s, occ_v));
-    if (c.blocks_per_sm > 0) per_sm = std::min(per_sm, c.blocks_per_sm);
-    std::vector<Item> items;
-    std::vector<int2> ranges;
-    build_schedule(shapes, TX, TY, c.kind, c.chunk, per_sm * num_sms_, &items, &ranges);
-    if (items.empty()) BAD("empty schedule");
-    for (const Item &it : items)
-      if (it.k1 <= it.k0) BAD("internal: empty work item");
-    nblocks_ = (int)ranges.size();
-    std::vector<ShotDesc<T>> descs;
-    std::vector<ShotMaps> maps;
-    for (auto &sp : shots_) { descs.push_back(sp->d); maps.push_back(sp->maps); }
-    CK(cudaMalloc(&d_desc_, descs.size() * sizeof(ShotDesc<T>)));
-    CK(cudaMalloc(&d_maps_, maps.size() * sizeof(ShotMaps)));
-    CK(cudaMalloc(&d_items_, items.size() * sizeof(Item)));
-    CK(cudaMalloc(&d_ranges_, ranges.size() * sizeof(int2)));
-    CK(cudaMemcpyAsync(d_desc_, descs.data(), descs.size() * sizeof(ShotDesc<T>), cudaMemcpyHostToDevice, stream_));
-    CK(cudaMemcpyAsync(d_maps_, maps.data(), maps.size() * sizeof(ShotMaps), cudaMemcpyHostToDevice, stream_));
-    CK(cudaMemcpyAsync(d_items_, items.data(), items.size() * sizeof(Item), cudaMemcpyHostToDevice, stream_));
-    CK(cudaMemcpyAsync(d_ranges_, ranges.data(), ranges.size() * sizeof(int2), cudaMemcpyHostToDevice, stream_));
-    CK(cudaStreamSynchronize(stream_));
+    per_sm_ = std::max(1, std::min(occ_s, occ_v));
+    if (c.blocks_per_sm > 0) per_sm_ = std::min(per_sm_, c.blocks_per_sm);
+    ela3d_status st = upload_tables();
+    if (st != ELA3D_OK) return st;
     finalized_ = true;
-    return ELA3D_OK;
+    return rebuild_schedule();
   }
 
-  ela3d_status launch_step(int tick) {
+  // Retire shots once they reach their nstep (batches with uneven lengths):
+  // their work items leave the schedule, their results stay readable.
+  void set_retire(bool on) override { retire_ = on; }
+
+  ela3d_status launch_step(int tick, const int *dtick) {
     int ctl = inject_ > 0 ? CTL_WITHHOLD_LOADS : 0;
     if (inject_ > 0) --inject_;
-    void *args[] = {&d_desc_, &d_maps_, &d_items_, &d_ranges_, &tick, &d_err_, &ctl};
+    void *args[] = {&d_desc_, &d_maps_, &d_items_, &d_ranges_, &tick, &dtick, &d_err_, &ctl};
     cudaEvent_t e0 = nullptr, e1 = nullptr, e2 = nullptr;
-    if (timing_) {
+    const bool timed = timing_ && !capturing_;
+    if (timed) {
       e0 = event(); e1 = event(); e2 = event();
       CK(cudaEventRecord(e0, stream_));
     }
     CK(cudaLaunchKernel(var_->stress, dim3(nblocks_), dim3(var_->threads), args, var_->stress_smem, stream_));
-    if (timing_) CK(cudaEventRecord(e1, stream_));
+    if (timed) CK(cudaEventRecord(e1, stream_));
     CK(cudaLaunchKernel(var_->velocity, dim3(nblocks_), dim3(var_->threads), args, var_->vel_smem, stream_));
-    if (timing_) {
+    if (timed) {
       CK(cudaEventRecord(e2, stream_));
       pending_.push_back({e0, e1, e2});
     }
-    if (any_explosive_) CK(Fp<T>::explosive(d_desc_, (int)shots_.size(), tick, stream_));
+    if (any_explosive_) CK(Fp<T>::explosive(d_desc_, (int)shots_.size(), tick, dtick, stream_));
+    launches_ += 2 + (any_explosive_ ? 1 : 0);
     return ELA3D_OK;
+  }
+
+  // Steps until the active set changes (a shot starts or reaches nstep).
+  int steps_to_boundary() const {
+    int best = 1 << 30;
+    for (auto &sp : shots_) {
+      const int start = sp->d.tick0 + 1, end = sp->d.tick0 + sp->p.nstep;  // ticks of its first/last step
+      if (tick_ + 1 < start) best = std::min(best, start - (tick_ + 1));
+      else if (tick_ + 1 <= end) best = std::min(best, end - tick_);
+    }
+    return best;
   }
 
   ela3d_status enqueue(int nsteps) override {
     if (!finalized_) BAD("engine not finalized");
     if (nsteps < 0) BAD("nsteps must be >= 0");
-    for (int s = 0; s < nsteps; ++s) {
-      ela3d_status st = launch_step(tick_ + 1);
-      if (st != ELA3D_OK) return st;
-      ++tick_;
+    while (nsteps > 0) {
+      int seg = nsteps;
+      if (retire_) {
+        ela3d_status st = rebuild_schedule();
+        if (st != ELA3D_OK) return st;
+        seg = std::min(seg, steps_to_boundary());
+        if (nblocks_ == 0) {  // nothing active: time passes, no work
+          tick_ += seg;
+          nsteps -= seg;
+          continue;
+        }
+      }
+      nsteps -= seg;
+      const bool graphs = use_graphs_ && !timing_ && inject_ == 0 && seg >= kGraphSteps;
+      if (graphs) {
+        ela3d_status st = ensure_graph();
+        if (st != ELA3D_OK) return st;
+        CK(launch_tick_set(d_tick_, tick_ + 1, stream_));
+        while (seg >= kGraphSteps) {
+          CK(cudaGraphLaunch(gexec_, stream_));
+          tick_ += kGraphSteps;
+          seg -= kGraphSteps;
+          launches_ += (int64_t)kGraphSteps * (2 + (any_explosive_ ? 1 : 0));
+        }
+      }
+      for (; seg > 0; --seg) {
+        ela3d_status st = launch_step(tick_ + 1, nullptr);
+        if (st != ELA3D_OK) return st;
+        ++tick_;
+      }
     }
+    return ELA3D_OK;
+  }
+
+  ela3d_status encode_shot_maps(Shot<T> &s) {
+    const int TX = var_->tx, TY = var_->ty, H = var_->halo;
+    ShotDesc<T> &d = s.d;
+    const int nx = d.nx, ny = d.ny, nz = d.nz, px = d.px;
+    CUtensorMap *m = s.maps.stress;
+    ela3d_status st;
+#define ENC(map, ptr, bw, bh) \
+  if ((st = encode_map<T>(map, ptr, nx, ny, nz, px, bw, bh)) != ELA3D_OK) return st
+    ENC(&m[0], d.f[0], TX + H, TY + 1);
+    ENC(&m[1], d.f[1], TX + H, TY + 1);
+    ENC(&m[2], d.f[2], TX + H, TY + 1);
+    ENC(&m[3], d.cs, TX + H, TY + 1);
+    ENC(&m[4], d.rho, TX + H, TY + 1);
+    ENC(&m[5], d.cp, TX, TY);
+    for (int q = 0; q < 6; ++q) ENC(&m[6 + q], d.f[3 + q], TX, TY);
+    CUtensorMap *v = s.maps.vel;
+    ENC(&v[0], d.f[3], TX + H, TY);      // sxx
+    ENC(&v[1], d.f[4], TX, TY + 1);      // syy
+    ENC(&v[2], d.f[5], TX, TY);          // szz
+    ENC(&v[3], d.f[6], TX + H, TY + 1);  // sxy
+    ENC(&v[4], d.f[7], TX + H, TY);      // sxz
+    ENC(&v[5], d.f[8], TX, TY + 1);      // syz
+    ENC(&v[6], d.rho, TX + H, TY + 1);   // rho
+    for (int q = 0; q < 3; ++q) ENC(&v[7 + q], d.f[q], TX, TY);
+#undef ENC
+    return ELA3D_OK;
+  }
+
+  // Shot descriptors and tensor maps to the device (once per composition).
+  ela3d_status upload_tables() {
+    std::vector<ShotDesc<T>> descs;
+    std::vector<ShotMaps> maps;
+    for (auto &sp : shots_) { descs.push_back(sp->d); maps.push_back(sp->maps); }
+    if (d_desc_) CK(cudaFree(d_desc_));
+    if (d_maps_) CK(cudaFree(d_maps_));
+    d_desc_ = nullptr;
+    d_maps_ = nullptr;
+    CK(cudaMalloc(&d_desc_, descs.size() * sizeof(ShotDesc<T>)));
+    CK(cudaMalloc(&d_maps_, maps.size() * sizeof(ShotMaps)));
+    CK(cudaMemcpyAsync(d_desc_, descs.data(), descs.size() * sizeof(ShotDesc<T>), cudaMemcpyHostToDevice, stream_));
+    CK(cudaMemcpyAsync(d_maps_, maps.data(), maps.size() * sizeof(ShotMaps), cudaMemcpyHostToDevice, stream_));
+    CK(cudaStreamSynchronize(stream_));
+    return ELA3D_OK;
+  }
+
+  // Work items for the shots active at the next step (all shots unless
+  // retirement is on).  Invalidates the cached graph when the split changes.
+  ela3d_status rebuild_schedule() {
+    std::vector<ShotShape> shapes;
+    std::vector<int> key;
+    for (int q = 0; q < (int)shots_.size(); ++q) {
+      const ShotDesc<T> &d = shots_[q]->d;
+      const int it = tick_ + 1 - d.tick0;
+      if (retire_ && (it < 1 || it > shots_[q]->p.nstep)) continue;
+      shapes.push_back({d.nx, d.ny, d.nz, q});
+      key.push_back(q);
+    }
+    if (!sched_key_.empty() && key == sched_key_ && sched_valid_) return ELA3D_OK;
+    sched_key_ = key;
+    sched_valid_ = true;
+    invalidate_graph();
+    if (shapes.empty()) {
+      nblocks_ = 0;
+      return ELA3D_OK;
+    }
+    std::vector<Item> items;
+    std::vector<int2> ranges;
+    build_schedule(shapes, var_->tx, var_->ty, choice_.kind, choice_.chunk, per_sm_ * num_sms_, &items, &ranges);
+    if (items.empty()) BAD("empty schedule");
+    for (const Item &it : items)
+      if (it.k1 <= it.k0) BAD("internal: empty work item");
+    CK(cudaStreamSynchronize(stream_));  // kernels in flight may still read the old tables
+    if (items.size() > items_cap_) {
+      if (d_items_) CK(cudaFree(d_items_));
+      d_items_ = nullptr;
+      CK(cudaMalloc(&d_items_, items.size() * sizeof(Item)));
+      items_cap_ = items.size();
+    }
+    if (ranges.size() > ranges_cap_) {
+      if (d_ranges_) CK(cudaFree(d_ranges_));
+      d_ranges_ = nullptr;
+      CK(cudaMalloc(&d_ranges_, ranges.size() * sizeof(int2)));
+      ranges_cap_ = ranges.size();
+    }
+    CK(cudaMemcpy(d_items_, items.data(), items.size() * sizeof(Item), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(d_ranges_, ranges.data(), ranges.size() * sizeof(int2), cudaMemcpyHostToDevice));
+    nblocks_ = (int)ranges.size();
+    nitems_ = (int)items.size();
+    return ELA3D_OK;
+  }
+
+  void invalidate_graph() {
+    if (gexec_) cudaGraphExecDestroy(gexec_);
+    gexec_ = nullptr;
+  }
+
+  // A replayable graph of kGraphSteps steps reading the step from d_tick_
+  // and advancing it at the end.
+  ela3d_status ensure_graph() {
+    if (gexec_) return ELA3D_OK;
+    CK(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
+    capturing_ = true;
+    ela3d_status st = ELA3D_OK;
+    for (int i = 0; i < kGraphSteps && st == ELA3D_OK; ++i) st = launch_step(i, d_tick_);
+    cudaError_t e = cudaSuccess;
+    if (st == ELA3D_OK) e = launch_tick_add(d_tick_, kGraphSteps, stream_);
+    cudaGraph_t g = nullptr;
+    cudaError_t e2 = cudaStreamEndCapture(stream_, &g);
+    capturing_ = false;
+    launches_ -= (int64_t)kGraphSteps * (2 + (any_explosive_ ? 1 : 0));  // counted when replayed
+    if (st != ELA3D_OK) { if (g) cudaGraphDestroy(g); return st; }
+    if (e != cudaSuccess || e2 != cudaSuccess) {
+      if (g) cudaGraphDestroy(g);
+      return status_from_cuda(e != cudaSuccess ? e : e2, "graph capture");
+    }
+    cudaError_t e3 = cudaGraphInstantiate(&gexec_, g, 0);
+    cudaGraphDestroy(g);
+    if (e3 != cudaSuccess) { gexec_ = nullptr; return status_from_cuda(e3, "cudaGraphInstantiate"); }
     return ELA3D_OK;
   }
 
@@ -703,9 +836,11 @@ class Engine final : public EngineBase {
     if (d_ranges_) cudaFree(d_ranges_);
     if (d_err_) cudaFree(d_err_);
     if (d_energy_) cudaFree(d_energy_);
+    if (d_tick_) cudaFree(d_tick_);
+    invalidate_graph();
     if (stream_) cudaStreamDestroy(stream_);
     d_desc_ = nullptr; d_maps_ = nullptr; d_items_ = nullptr; d_ranges_ = nullptr;
-    d_err_ = nullptr; d_energy_ = nullptr; stream_ = nullptr;
+    d_err_ = nullptr; d_energy_ = nullptr; d_tick_ = nullptr; stream_ = nullptr;
   }
 
   struct Ev { cudaEvent_t e0, e1, e2; };
@@ -721,9 +856,17 @@ class Engine final : public EngineBase {
   int2 *d_ranges_ = nullptr;
   unsigned *d_err_ = nullptr;
   double *d_energy_ = nullptr;
-  int nblocks_ = 0;
+  int nblocks_ = 0, nitems_ = 0, per_sm_ = 1;
+  size_t items_cap_ = 0, ranges_cap_ = 0;
+  std::vector<int> sched_key_;
+  bool sched_valid_ = false, retire_ = false;
   int tick_ = 0;
-  int inject_ = 0;   // launches left that withhold their loads (test hook)
+  int inject_ = 0;   // steps left whose launches withhold their loads (test hook)
+  int *d_tick_ = nullptr;
+  cudaGraphExec_t gexec_ = nullptr;
+  bool use_graphs_ = true, capturing_ = false;
+  int64_t launches_ = 0;
+  static constexpr int kGraphSteps = 50;
   bool timing_ = false;
   std::vector<Ev> pending_;
   std::vector<cudaEvent_t> free_events_;

@@ -32,9 +32,11 @@ void slab_extent(const double *a_full, const double *a_half, int n, int *lo, int
 // contiguous, equal share of the units in (shot, tile, plane) order; kind 1
 // splits each tile column into z-chunks of `chunk` planes and deals the
 // chunks round-robin in (shot, chunk, tile) order so that blocks running at
-// the same time work on neighbouring tiles.
+// the same time work on neighbouring tiles; kind 2 deals them in
+// (chunk, tile, shot) order (same tile of many shots at once).
 struct ShotShape {
   int nx, ny, nz;
+  int id = -1;   // shot index written into the items (-1: position in the list)
 };
 void build_schedule(const std::vector<ShotShape> &shots, int tx, int ty, int kind, int chunk,
                     int max_blocks, std::vector<Item> *items, std::vector<int2> *ranges);
@@ -64,6 +66,7 @@ class EngineBase {
   virtual ela3d_status info(int shot, ela3d_plan_info *out) = 0;
   virtual ela3d_status set_timing(bool on) = 0;
   virtual ela3d_status inject_timeout(int launches) = 0;
+  virtual void set_retire(bool on) = 0;
   virtual ela3d_status timing(double *s_ms, double *v_ms, int64_t *ns, int64_t *nv) = 0;
   virtual int nshots() const = 0;
   virtual int steps_done() const = 0;

@@ -49,8 +49,13 @@ cudaError_t launch_stf_f64(const StfArgs &a, double *out, cudaStream_t s);
 cudaError_t launch_pad_f32(const float *src, float *dst, int nx, int ny, int nz, int px, cudaStream_t s);
 cudaError_t launch_pad_f64(const float *src, double *dst, int nx, int ny, int nz, int px, cudaStream_t s);
 // Explosive source after the velocity half-step, one thread per shot.
-cudaError_t launch_explosive_f32(const ShotDesc<float> *shots, int nshots, int tick, cudaStream_t s);
-cudaError_t launch_explosive_f64(const ShotDesc<double> *shots, int nshots, int tick, cudaStream_t s);
+cudaError_t launch_explosive_f32(const ShotDesc<float> *shots, int nshots, int tick, const int *dtick,
+                                 cudaStream_t s);
+cudaError_t launch_explosive_f64(const ShotDesc<double> *shots, int nshots, int tick, const int *dtick,
+                                 cudaStream_t s);
+// Device step counter of replayable graphs: *dtick = value / *dtick += delta.
+cudaError_t launch_tick_set(int *dtick, int value, cudaStream_t s);
+cudaError_t launch_tick_add(int *dtick, int delta, cudaStream_t s);
 // Total energy of one shot, accumulated into *out (double, device).
 cudaError_t launch_energy_f32(const ShotDesc<float> *shot, int nx, int ny, int nz, double *out, cudaStream_t s);
 cudaError_t launch_energy_f64(const ShotDesc<double> *shot, int nx, int ny, int nz, double *out, cudaStream_t s);

@@ -119,11 +119,13 @@ __device__ __forceinline__ void produce(const Item *__restrict__ items, int2 ran
 }
 
 // ----------------------------------------------------------- stress ----
+// (tick and dtick are unused by the stress half-step; the parameter list is
+// shared with the velocity kernel so both launch from one argument array)
 template <typename T, int TX, int TY, int NS>
 __global__ void __launch_bounds__(Geo<T, TX, TY, NS>::THREADS, Geo<T, TX, TY, NS>::MINB)
     stress_kernel(const ShotDesc<T> *__restrict__ shots, const ShotMaps *__restrict__ maps,
                   const Item *__restrict__ items, const int2 *__restrict__ ranges, int tick,
-                  unsigned *__restrict__ err, int ctl) {
+                  const int *__restrict__ dtick, unsigned *__restrict__ err, int ctl) {
   using G = Geo<T, TX, TY, NS>;
   constexpr int V = G::VEC, H = G::H, WW = G::WW;
   extern __shared__ __align__(1024) unsigned char smem[];
@@ -438,7 +440,7 @@ template <typename T, int TX, int TY, int NS>
 __global__ void __launch_bounds__(Geo<T, TX, TY, NS>::THREADS, Geo<T, TX, TY, NS>::MINB)
     velocity_kernel(const ShotDesc<T> *__restrict__ shots, const ShotMaps *__restrict__ maps,
                     const Item *__restrict__ items, const int2 *__restrict__ ranges, int tick,
-                    unsigned *__restrict__ err, int ctl) {
+                    const int *__restrict__ dtick, unsigned *__restrict__ err, int ctl) {
   using G = Geo<T, TX, TY, NS>;
   constexpr int V = G::VEC, H = G::H, WW = G::WW;
   extern __shared__ __align__(1024) unsigned char smem[];
@@ -485,6 +487,9 @@ __global__ void __launch_bounds__(Geo<T, TX, TY, NS>::THREADS, Geo<T, TX, TY, NS
   const int tx = tid % G::NTX, ty = tid / G::NTX;
   const unsigned long long wait_ns = ctl ? kTestWaitLimitNs : kWaitLimitNs;
   constexpr int CS = G::SC / (int)sizeof(T);
+  // step counter: an argument for direct launches, device memory plus an
+  // offset inside a replayable CUDA graph
+  if (dtick) tick += *dtick;
   long long n = 0;
 
   for (int ii = range.x; ii < range.y; ++ii) {

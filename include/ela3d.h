@@ -195,6 +195,28 @@ ela3d_status ela3d_variant_get(int32_t index, ela3d_variant_info *out);
 ela3d_status ela3d_plan_create_tuned(const ela3d_params *p, const float *cp, const float *cs,
                                      const float *rho, const ela3d_tuning *tune, ela3d_plan **out);
 
+/* ---- batches of shots ---------------------------------------------------- */
+/* Many shots resident together and advanced by the same two launches per
+ * time step (the persistent kernels deal (shot, tile, z-run) items to all
+ * SMs).  Shots may differ in size, model, source, receivers, dt and nstep
+ * (same precision).  Shots whose cp, cs and rho pointers and grid equal an
+ * earlier shot's share that shot's device model.  A shot stops being
+ * computed once it has done its nstep steps; its results stay readable.
+ * Runs of 50 or more steps replay a captured CUDA graph.  The reference runs
+ * one shot per process (no counterpart). */
+typedef struct ela3d_batch ela3d_batch;
+ela3d_status ela3d_batch_create(int32_t nshots, const ela3d_params *params, const float *const *cp,
+                                const float *const *cs, const float *const *rho, const ela3d_tuning *tune,
+                                ela3d_batch **out);
+/* Advances every unfinished shot by up to nsteps steps and waits. */
+ela3d_status ela3d_batch_run(ela3d_batch *b, int32_t nsteps);
+/* ela3d_batch_run timed with CUDA events on the batch's stream. */
+ela3d_status ela3d_batch_run_timed(ela3d_batch *b, int32_t nsteps, double *ms);
+ela3d_status ela3d_batch_get_seismograms(ela3d_batch *b, int32_t shot, float *out);
+ela3d_status ela3d_batch_get_field(ela3d_batch *b, int32_t shot, int32_t comp, float *out);
+ela3d_status ela3d_batch_info(ela3d_batch *b, int32_t shot, ela3d_plan_info *out);
+ela3d_status ela3d_batch_destroy(ela3d_batch *b);
+
 /* ---- host-side planning (no GPU needed) ---------------------------------- */
 /* C-PML slab extent of one axis from its 'a' profiles: cells [0, lo) and
  * [hi, n) may carry memory variables; every cell of [lo, hi) has a = 0 in
