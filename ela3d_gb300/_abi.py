@@ -50,6 +50,16 @@ SIGNATURES = [
     ("ela3d_batch_get_field", _c.c_int, [_P, _c.c_int32, _c.c_int32, _P]),
     ("ela3d_batch_info", _c.c_int, [_P, _c.c_int32, _P]),
     ("ela3d_batch_destroy", _c.c_int, [_P]),
+    ("ela3d_server_config_default", _c.c_int, [_P]),
+    ("ela3d_server_create", _c.c_int, [_P, _c.POINTER(_P)]),
+    ("ela3d_server_submit", _c.c_int, [_P, _c.POINTER(CParams), _P, _P, _P, _c.POINTER(_c.c_uint64)]),
+    ("ela3d_server_poll", _c.c_int, [_P, _c.c_uint64, _c.POINTER(_c.c_int32), _c.POINTER(_c.c_int32)]),
+    ("ela3d_server_read", _c.c_int, [_P, _c.c_uint64, _c.c_int32, _c.c_int32, _P]),
+    ("ela3d_server_wait", _c.c_int, [_P, _c.c_uint64, _c.c_int32]),
+    ("ela3d_server_cancel", _c.c_int, [_P, _c.c_uint64]),
+    ("ela3d_server_release", _c.c_int, [_P, _c.c_uint64]),
+    ("ela3d_server_stats_get", _c.c_int, [_P, _P]),
+    ("ela3d_server_destroy", _c.c_int, [_P]),
     ("ela3d_variant_count", _c.c_int32, []),
     ("ela3d_variant_get", _c.c_int, [_c.c_int32, _P]),
     ("ela3d_plan_create_tuned", _c.c_int, [_c.POINTER(CParams), _P, _P, _P, _P, _c.POINTER(_P)]),
@@ -308,6 +318,105 @@ class Batch:
     def close(self) -> None:
         if getattr(self, "_h", None) is not None and self._h.value:
             self._lib.ela3d_batch_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("hbm_budget_bytes", ctypes.c_int64), ("max_active", ctypes.c_int32),
+                ("steps_per_round", ctypes.c_int32), ("precision", ctypes.c_int32), ("_pad", ctypes.c_int32),
+                ("tune", Tuning)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("submitted", ctypes.c_int64), ("completed", ctypes.c_int64), ("failed", ctypes.c_int64),
+                ("cancelled", ctypes.c_int64), ("queued", ctypes.c_int64), ("running", ctypes.c_int64),
+                ("rounds", ctypes.c_int64), ("cell_updates", ctypes.c_double), ("busy_seconds", ctypes.c_double),
+                ("wall_seconds", ctypes.c_double), ("latency_p50_s", ctypes.c_double),
+                ("latency_p99_s", ctypes.c_double), ("latency_max_s", ctypes.c_double),
+                ("device_bytes_in_use", ctypes.c_int64), ("device_bytes_budget", ctypes.c_int64)]
+
+    def as_dict(self) -> dict:
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_FAILED, REQ_CANCELLED = range(5)
+
+
+class Server:
+    """Continuous-batching request loop (ela3d_server_*)."""
+
+    def __init__(self, hbm_budget_bytes: int = 0, max_active: int = 0, steps_per_round: int = 50,
+                 precision: int = 0, variant: int = -1, schedule: int = -1, chunk: int = 0):
+        lib = load_library()
+        self._lib = lib
+        cfg = ServerConfig()
+        _check(lib.ela3d_server_config_default(ctypes.byref(cfg)), "ela3d_server_config_default")
+        cfg.hbm_budget_bytes = hbm_budget_bytes
+        cfg.max_active = max_active
+        cfg.steps_per_round = steps_per_round
+        cfg.precision = precision
+        cfg.tune = Tuning(variant, schedule, chunk, -1)
+        h = ctypes.c_void_p()
+        _check(lib.ela3d_server_create(ctypes.byref(cfg), ctypes.byref(h)), "ela3d_server_create")
+        self._h = h
+        self._params = {}
+
+    def submit(self, params: ShotParams, cp, cs, rho) -> int:
+        c, rec = params.to_c()
+        m = [np.ascontiguousarray(a, dtype=np.float32).reshape(-1) for a in (cp, cs, rho)]
+        if any(x.size != params.cells for x in m):
+            raise ValueError("model arrays must hold nx*ny*nz float32 values")
+        t = ctypes.c_uint64()
+        _check(self._lib.ela3d_server_submit(self._h, ctypes.byref(c), m[0].ctypes.data, m[1].ctypes.data,
+                                             m[2].ctypes.data, ctypes.byref(t)), "ela3d_server_submit")
+        self._params[t.value] = params
+        return t.value
+
+    def poll(self, ticket: int) -> tuple[int, int]:
+        st, ready = ctypes.c_int32(), ctypes.c_int32()
+        rc = self._lib.ela3d_server_poll(self._h, ticket, ctypes.byref(st), ctypes.byref(ready))
+        if rc not in (0,) and st.value != REQ_FAILED:
+            _check(rc, "ela3d_server_poll")
+        return st.value, ready.value
+
+    def read(self, ticket: int, first: int = 0, count: int | None = None) -> np.ndarray:
+        p = self._params[ticket]
+        count = p.nsamp - first if count is None else count
+        out = np.zeros((p.nrec, 3, count), np.float32)
+        if out.size:
+            _check(self._lib.ela3d_server_read(self._h, ticket, first, count, out.ctypes.data), "ela3d_server_read")
+        return out
+
+    def wait(self, ticket: int, timeout_ms: int = -1) -> None:
+        _check(self._lib.ela3d_server_wait(self._h, ticket, timeout_ms), "ela3d_server_wait")
+
+    def cancel(self, ticket: int) -> None:
+        _check(self._lib.ela3d_server_cancel(self._h, ticket), "ela3d_server_cancel")
+
+    def release(self, ticket: int) -> None:
+        _check(self._lib.ela3d_server_release(self._h, ticket), "ela3d_server_release")
+        self._params.pop(ticket, None)
+
+    def stats(self) -> dict:
+        s = ServerStats()
+        _check(self._lib.ela3d_server_stats_get(self._h, ctypes.byref(s)), "ela3d_server_stats_get")
+        return s.as_dict()
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) is not None and self._h.value:
+            self._lib.ela3d_server_destroy(self._h)
             self._h = ctypes.c_void_p()
 
     def __enter__(self):

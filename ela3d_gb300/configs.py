@@ -12,9 +12,9 @@
 - uneven_batch: 48 grids with edges drawn from multiples of 16 in [64, 320]
   (numpy default_rng(1)), random 3-6 layer domes, npml U{10..20}, dt half
   the CFL limit, nstep reaching t = 2 s.
-- serving_requests: request stream with lognormal edges clipped to
+- serving_request: one request of a stream with lognormal edges clipped to
   [64, 384] (mu = ln 128, sigma = 0.45), per-request seed for model, source
-  and receiver line.
+  and receiver line; npml U{10..20}, at most (min edge - 10) / 2.
 Edge lengths, positions and seeds are those the configs name; anything they
 leave open is fixed here and stated in the docstring.
 """
@@ -103,7 +103,7 @@ def serving_request(seed: int, t_end: float = 2.0, precision: int = FP32, lo: in
     rng = np.random.default_rng(seed)
     edges = [int(min(max(round(rng.lognormal(mu, sigma)), lo), hi)) for _ in range(3)]
     nx, ny, nz = edges
-    npml = int(rng.integers(10, 21))
+    npml = min(int(rng.integers(10, 21)), (min(edges) - 10) // 2)
     cp, cs, rho = media.random_anticline(rng, nx, ny, nz)
     dt = cfl_dt(float(cp.max()), 10.0, 10.0, 10.0, 0.5)
     nstep = int(math.ceil(t_end / dt))

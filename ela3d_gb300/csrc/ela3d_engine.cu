@@ -194,6 +194,7 @@ struct Shot {
   ShotDesc<T> d{};
   ShotMaps maps{};
   double e_ref = -1.0; // energy monitor reference after the source ended
+  uint64_t key = 0;    // stable identity while shots join and leave
 };
 
 template <typename T> struct Fp;
@@ -250,7 +251,6 @@ class Engine final : public EngineBase {
 
   ela3d_status add_shot(const ela3d_params &p, const float *cp, const float *cs, const float *rho,
                         int shared_model_of) override {
-    if (finalized_) BAD("engine already finalized");
     ela3d_status st = validate_params(p);
     if (st != ELA3D_OK) return st;
     if ((p.precision == ELA3D_FP64) != (sizeof(T) == 8)) BAD("precision does not match the engine");
@@ -347,7 +347,7 @@ class Engine final : public EngineBase {
 
     ShotDesc<T> &d = s.d;
     d.nx = nx; d.ny = ny; d.nz = nz; d.px = px;
-    d.tick0 = 0;
+    d.tick0 = tick_;   // its first step is the engine's next step
     d.nstep = p.nstep;
     d.xl = xl; d.xr = xr; d.xw = xw;
     d.yl = yl; d.yr = yr; d.yw = yw;
@@ -430,12 +430,105 @@ class Engine final : public EngineBase {
     }
     if (p.src_kind == ELA3D_SRC_EXPLOSIVE) any_explosive_ = true;
     shots_.push_back(std::move(sh));
+    if (finalized_) {  // a shot joining a running engine
+      Shot<T> &ns = *shots_.back();
+      ns.key = next_key_++;
+      ela3d_status st2 = encode_shot_maps(ns);
+      if (st2 == ELA3D_OK) st2 = upload_tables();
+      if (st2 != ELA3D_OK) {
+        release_shot(ns);
+        shots_.pop_back();
+        return st2;
+      }
+      sched_valid_ = false;
+    } else {
+      shots_.back()->key = next_key_++;
+    }
     return ELA3D_OK;
+  }
+
+  uint64_t last_key() const override { return shots_.empty() ? 0 : shots_.back()->key; }
+
+  int index_of(uint64_t key) const {
+    for (int q = 0; q < (int)shots_.size(); ++q)
+      if (shots_[q]->key == key) return q;
+    return -1;
+  }
+
+  ela3d_status remove_shot(uint64_t key) override {
+    const int q = index_of(key);
+    if (q < 0) {
+      set_last_error("no such shot");
+      return ELA3D_ERR_NOT_FOUND;
+    }
+    for (auto &sp : shots_)
+      if (sp->model_of == q) BAD("another shot shares this shot's model");
+    CK(cudaStreamSynchronize(stream_));
+    release_shot(*shots_[q]);
+    shots_.erase(shots_.begin() + q);
+    for (auto &sp : shots_)
+      if (sp->model_of > q) --sp->model_of;
+    any_explosive_ = false;
+    for (auto &sp : shots_) any_explosive_ |= sp->p.src_kind == ELA3D_SRC_EXPLOSIVE;
+    sched_valid_ = false;
+    if (shots_.empty()) {
+      invalidate_graph();
+      nblocks_ = 0;
+      return ELA3D_OK;
+    }
+    return upload_tables();
+  }
+
+  // Device bytes add_shot would allocate for p (slabs estimated from npml,
+  // an upper bound of the exact profile-derived extents).
+  int64_t footprint(const ela3d_params &p) const override {
+    constexpr int kAlign = 128 / (int)sizeof(T), V = Vec<T>::N;
+    const int64_t px = (p.nx + kAlign - 1) / kAlign * kAlign;
+    const int64_t cells = px * p.ny * p.nz;
+    const int64_t w = 2 * (p.npml + 1);
+    const int64_t xw = std::min<int64_t>(px, w + 2 * V), yw = std::min<int64_t>(p.ny, w), zw = std::min<int64_t>(p.nz, w);
+    int64_t b = 12 * cells + 6 * ((int64_t)p.nz * p.ny * xw + (int64_t)p.nz * yw * px + zw * (int64_t)p.ny * px);
+    b = b * (int64_t)sizeof(T) + (int64_t)p.nrec * 3 * (p.nstep / std::max(1, p.sampgat)) * (int64_t)sizeof(T) +
+        (int64_t)p.nstep * (int64_t)sizeof(T) + 6 * (px + p.ny + p.nz) * (int64_t)sizeof(T) + 32 * 256;
+    return b;
+  }
+
+  int shot_steps(uint64_t key) const override {
+    const int q = index_of(key);
+    if (q < 0) return -1;
+    return std::min(tick_ - shots_[q]->d.tick0, shots_[q]->p.nstep);
+  }
+
+  // Samples [from, to) of every trace of a shot into host memory laid out
+  // [nrec][3][to - from].
+  ela3d_status read_samples(uint64_t key, int from, int to, float *out) override {
+    const int q = index_of(key);
+    if (q < 0) {
+      set_last_error("no such shot");
+      return ELA3D_ERR_NOT_FOUND;
+    }
+    const Shot<T> &s = *shots_[q];
+    if (from < 0 || to > s.nsamp || from > to) BAD("sample range");
+    const int n = to - from, rows = s.p.nrec * 3;
+    if (n == 0 || rows == 0) return ELA3D_OK;
+    std::vector<T> h((size_t)rows * n);
+    CK(cudaMemcpy2DAsync(h.data(), n * sizeof(T), s.d.seis + from, s.nsamp * sizeof(T), n * sizeof(T), rows,
+                         cudaMemcpyDeviceToHost, stream_));
+    CK(cudaStreamSynchronize(stream_));
+    for (size_t i = 0; i < h.size(); ++i) out[i] = (float)h[i];
+    return ELA3D_OK;
+  }
+
+  void release_shot(Shot<T> &s) {
+    if (s.pool) cudaFree(s.pool);
+    if (s.prof) cudaFree(s.prof);
+    s.pool = nullptr;
+    s.prof = nullptr;
   }
 
   ela3d_status finalize(const TuneChoice *choice) override {
     if (finalized_) return ELA3D_OK;
-    if (shots_.empty()) BAD("no shots");
+    if (shots_.empty() && !choice) BAD("no shots");
     int nv = 0;
     const Variant *vs = variants(&nv);
     TuneChoice c = choice ? *choice : default_choice(sizeof(T) == 8, shots_[0]->p.nx, shots_[0]->p.ny, shots_[0]->p.nz);
@@ -453,8 +546,10 @@ class Engine final : public EngineBase {
     CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_v, var_->velocity, var_->threads, var_->vel_smem));
     per_sm_ = std::max(1, std::min(occ_s, occ_v));
     if (c.blocks_per_sm > 0) per_sm_ = std::min(per_sm_, c.blocks_per_sm);
-    ela3d_status st = upload_tables();
-    if (st != ELA3D_OK) return st;
+    if (!shots_.empty()) {
+      ela3d_status st = upload_tables();
+      if (st != ELA3D_OK) return st;
+    }
     finalized_ = true;
     return rebuild_schedule();
   }
@@ -512,6 +607,10 @@ class Engine final : public EngineBase {
         }
       }
       nsteps -= seg;
+      if (nblocks_ == 0) {
+        tick_ += seg;
+        continue;
+      }
       const bool graphs = use_graphs_ && !timing_ && inject_ == 0 && seg >= kGraphSteps;
       if (graphs) {
         ela3d_status st = ensure_graph();
@@ -746,6 +845,14 @@ class Engine final : public EngineBase {
     return ELA3D_OK;
   }
 
+  int64_t launches() const override { return launches_; }
+
+  int64_t device_bytes() const override {
+    int64_t b = 0;
+    for (auto &sp : shots_) b += (int64_t)(sp->pool_bytes + sp->prof_bytes);
+    return b;
+  }
+
   ela3d_status set_timing(bool on) override {
     timing_ = on;
     if (on) { t_stress_ = t_vel_ = 0.0; n_stress_ = n_vel_ = 0; }
@@ -821,10 +928,7 @@ class Engine final : public EngineBase {
 
   void release() {
     if (stream_) cudaStreamSynchronize(stream_);
-    for (auto &sp : shots_) {
-      if (sp->pool) cudaFree(sp->pool);
-      if (sp->prof) cudaFree(sp->prof);
-    }
+    for (auto &sp : shots_) release_shot(*sp);
     shots_.clear();
     for (auto &t : pending_) { cudaEventDestroy(t.e0); cudaEventDestroy(t.e1); cudaEventDestroy(t.e2); }
     for (auto e : free_events_) cudaEventDestroy(e);
@@ -866,6 +970,7 @@ class Engine final : public EngineBase {
   cudaGraphExec_t gexec_ = nullptr;
   bool use_graphs_ = true, capturing_ = false;
   int64_t launches_ = 0;
+  uint64_t next_key_ = 1;
   static constexpr int kGraphSteps = 50;
   bool timing_ = false;
   std::vector<Ev> pending_;

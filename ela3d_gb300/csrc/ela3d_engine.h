@@ -67,6 +67,14 @@ class EngineBase {
   virtual ela3d_status set_timing(bool on) = 0;
   virtual ela3d_status inject_timeout(int launches) = 0;
   virtual void set_retire(bool on) = 0;
+  // live composition (serving): shots may join after finalize and leave
+  virtual uint64_t last_key() const = 0;  // key of the most recently added shot
+  virtual ela3d_status remove_shot(uint64_t key) = 0;
+  virtual int64_t footprint(const ela3d_params &p) const = 0;
+  virtual int shot_steps(uint64_t key) const = 0;
+  virtual ela3d_status read_samples(uint64_t key, int from, int to, float *out) = 0;
+  virtual int64_t launches() const = 0;
+  virtual int64_t device_bytes() const = 0;
   virtual ela3d_status timing(double *s_ms, double *v_ms, int64_t *ns, int64_t *nv) = 0;
   virtual int nshots() const = 0;
   virtual int steps_done() const = 0;

@@ -217,6 +217,58 @@ ela3d_status ela3d_batch_get_field(ela3d_batch *b, int32_t shot, int32_t comp, f
 ela3d_status ela3d_batch_info(ela3d_batch *b, int32_t shot, ela3d_plan_info *out);
 ela3d_status ela3d_batch_destroy(ela3d_batch *b);
 
+/* ---- serving: continuous batching ---------------------------------------- */
+/* A request loop on one GPU.  Shot requests of any size are queued and
+ * admitted in arrival order while their device footprint fits the budget
+ * (and a slot is free); admitted shots stay resident and are advanced
+ * together by the batched kernels, `steps_per_round` steps per round;
+ * requests arriving meanwhile join at the next round, and finished shots
+ * leave, freeing memory.  Seismogram samples are copied back after every
+ * round and can be read while the shot runs.  A request whose footprint
+ * exceeds the whole budget fails with ELA3D_ERR_BUSY.  No reference
+ * counterpart (the reference runs one hard-coded shot per process). */
+typedef struct ela3d_server ela3d_server;
+typedef struct ela3d_server_config {
+    int64_t hbm_budget_bytes;   /* device bytes for shot state; 0 = 80% of free memory */
+    int32_t max_active;         /* concurrent shots; 0 = no limit */
+    int32_t steps_per_round;    /* time steps between admission rounds (default 50) */
+    int32_t precision;          /* of every request */
+    int32_t _pad;
+    ela3d_tuning tune;
+} ela3d_server_config;
+/* Request states reported by ela3d_server_poll. */
+enum { ELA3D_REQ_QUEUED = 0, ELA3D_REQ_RUNNING = 1, ELA3D_REQ_DONE = 2, ELA3D_REQ_FAILED = 3,
+       ELA3D_REQ_CANCELLED = 4 };
+typedef struct ela3d_server_stats {
+    int64_t submitted, completed, failed, cancelled, queued, running, rounds;
+    double cell_updates;        /* of completed requests */
+    double busy_seconds;        /* wall time of the device rounds */
+    double wall_seconds;        /* first submission to last completion */
+    double latency_p50_s, latency_p99_s, latency_max_s;  /* submission to completion */
+    int64_t device_bytes_in_use, device_bytes_budget;
+} ela3d_server_stats;
+
+ela3d_status ela3d_server_config_default(ela3d_server_config *c);
+/* Starts the worker thread on the calling thread's current device. */
+ela3d_status ela3d_server_create(const ela3d_server_config *cfg, ela3d_server **out);
+/* Queues one shot; the parameters, receivers and model are copied. */
+ela3d_status ela3d_server_submit(ela3d_server *s, const ela3d_params *p, const float *cp, const float *cs,
+                                 const float *rho, uint64_t *ticket);
+/* State and number of seismogram samples available so far. */
+ela3d_status ela3d_server_poll(ela3d_server *s, uint64_t ticket, int32_t *state, int32_t *samples_ready);
+/* Samples [first, first+count) of every trace, [nrec][3][count]; returns
+ * ELA3D_ERR_NOT_READY if they have not all arrived. */
+ela3d_status ela3d_server_read(ela3d_server *s, uint64_t ticket, int32_t first, int32_t count, float *out);
+/* Waits for a request to finish (timeout_ms < 0: no limit). */
+ela3d_status ela3d_server_wait(ela3d_server *s, uint64_t ticket, int32_t timeout_ms);
+/* Stops a queued or running request at the next round boundary. */
+ela3d_status ela3d_server_cancel(ela3d_server *s, uint64_t ticket);
+/* Forgets a finished request (frees its host results). */
+ela3d_status ela3d_server_release(ela3d_server *s, uint64_t ticket);
+ela3d_status ela3d_server_stats_get(ela3d_server *s, ela3d_server_stats *out);
+/* Stops the worker; running requests are abandoned. */
+ela3d_status ela3d_server_destroy(ela3d_server *s);
+
 /* ---- host-side planning (no GPU needed) ---------------------------------- */
 /* C-PML slab extent of one axis from its 'a' profiles: cells [0, lo) and
  * [hi, n) may carry memory variables; every cell of [lo, hi) has a = 0 in

@@ -1,0 +1,128 @@
+"""Serving with continuous batching: each request's result is the same alone
+and in the mix (bit-identical: the per-cell arithmetic does not depend on
+which shots share the launches), with requests arriving while others run,
+cancellations, an oversize request and a small device budget."""
+import threading
+import time
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def request(seed, t_end=0.12):
+    from ela3d_gb300 import configs
+
+    return configs.serving_request(seed, t_end=t_end, lo=40, hi=96)
+
+
+def alone(p, cp, cs, rho):
+    from ela3d_gb300 import Plan
+
+    with Plan(p, cp, cs, rho, variant=0) as plan:
+        plan.run(p.nstep)
+        return plan.seismograms()
+
+
+def test_mix_equals_alone_with_late_arrivals(built):
+    from ela3d_gb300 import Server
+
+    reqs = [request(s) for s in range(8)]
+    want = [alone(*r) for r in reqs]
+    with Server(steps_per_round=37, variant=0) as srv:
+        tickets = [srv.submit(*reqs[q]) for q in range(4)]
+        time.sleep(0.05)                     # the first four are running
+        tickets += [srv.submit(*reqs[q]) for q in range(4, 8)]
+        for q, t in enumerate(tickets):
+            srv.wait(t)
+            assert np.array_equal(srv.read(t), want[q]), q
+        st = srv.stats()
+    assert st["completed"] == 8 and st["failed"] == 0
+    assert st["latency_p99_s"] >= st["latency_p50_s"] > 0
+    assert st["rounds"] > 1
+
+
+def test_streaming_samples_arrive_before_completion(built):
+    from ela3d_gb300 import Server
+    from ela3d_gb300._abi import REQ_DONE, REQ_RUNNING
+
+    p, cp, cs, rho = request(11, t_end=0.25)
+    want = alone(p, cp, cs, rho)
+    seen_partial = False
+    with Server(steps_per_round=20, variant=0) as srv:
+        t = srv.submit(p, cp, cs, rho)
+        got = np.zeros_like(want)
+        done = 0
+        while True:
+            state, ready = srv.poll(t)
+            if ready > done:
+                got[:, :, done:ready] = srv.read(t, done, ready - done)
+                if state == REQ_RUNNING:
+                    seen_partial = True
+                done = ready
+            if state == REQ_DONE and done == p.nsamp:
+                break
+            time.sleep(0.002)
+    assert seen_partial
+    assert np.array_equal(got, want)
+
+
+def test_cancel_and_oversize_leave_others_identical(built):
+    from ela3d_gb300 import Ela3dError, Server
+
+    reqs = [request(s) for s in range(20, 26)]
+    want = [alone(*r) for r in reqs]
+    with Server(steps_per_round=25, variant=0, hbm_budget_bytes=256 << 20) as srv:
+        big = request(99)
+        big_p = big[0].with_(nx=400, ny=400, nz=200, rec=np.zeros((0, 3), np.int32), src=(5, 5, 5))
+        n = big_p.cells
+        m = np.ones(n, np.float32)
+        t_big = srv.submit(big_p, m * 3000, m * 1700, m * 2000)
+        tickets = [srv.submit(*r) for r in reqs]
+        srv.cancel(tickets[2])
+        with pytest.raises(Ela3dError) as e:
+            srv.wait(t_big)
+        assert e.value.status == 7   # ELA3D_ERR_BUSY: larger than the whole budget
+        for q, t in enumerate(tickets):
+            if q == 2:
+                with pytest.raises(Ela3dError):
+                    srv.wait(t)
+                continue
+            srv.wait(t)
+            assert np.array_equal(srv.read(t), want[q]), q
+        st = srv.stats()
+    assert st["cancelled"] == 1 and st["failed"] == 1 and st["completed"] == 5
+
+
+def test_small_budget_serialises_admission(built):
+    from ela3d_gb300 import Server
+
+    reqs = [request(s) for s in range(40, 44)]
+    want = [alone(*r) for r in reqs]
+    with Server(steps_per_round=30, variant=0, max_active=1) as srv:
+        tickets = [srv.submit(*r) for r in reqs]
+        for q, t in enumerate(tickets):
+            srv.wait(t)
+            assert np.array_equal(srv.read(t), want[q])
+
+
+def test_concurrent_clients(built):
+    from ela3d_gb300 import Server
+
+    reqs = [request(s) for s in range(60, 66)]
+    want = [alone(*r) for r in reqs]
+    out = [None] * len(reqs)
+    with Server(steps_per_round=40, variant=0) as srv:
+        def client(q):
+            t = srv.submit(*reqs[q])
+            srv.wait(t)
+            out[q] = srv.read(t)
+            srv.release(t)
+        th = [threading.Thread(target=client, args=(q,)) for q in range(len(reqs))]
+        for x in th:
+            x.start()
+        for x in th:
+            x.join()
+    for q in range(len(reqs)):
+        assert np.array_equal(out[q], want[q])
