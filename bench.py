@@ -17,8 +17,9 @@ over ranks.  Also reported:
   cpu_baseline  the reference CPU program (oracle/_ref, else the oracle's C
             restatement) on 1 core, a bounded sample of the same shot.
 Also in the same line: "batched" (64 shots of the 256^3 anticline sharing
-one model, advanced together) and "uneven" (48 uneven grids together vs one
-at a time), each next to the single-shot path on the same GPU.
+one model, advanced together), "uneven" (48 uneven grids together vs one
+at a time) and "serving" (a Poisson request stream swept to saturation,
+p50/p99 latency), each next to the single-shot path on the same GPU.
 Reference arm (--impl reference): the reference CPU program itself on all
 host cores (one process per core, each a bounded sample of the same shot),
 rank 0 only.
@@ -321,6 +322,7 @@ def run_ours(args, rank, world, local):
     if not args.no_batched:
         extra["batched"] = batched_shots(args, value)
         extra["uneven"] = uneven_batch(args)
+        extra["serving"] = serving(args)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -400,6 +402,78 @@ def uneven_batch(args) -> dict:
             "timing": "CUDA events; the same steps of every instance, batched vs one plan at a time"}
 
 
+def serving(args) -> dict:
+    """Request stream with Poisson arrivals, swept to saturation.  Requests
+    are seeded draws of configs.serving_request (lognormal edges in
+    [64, 384]); the stream is a bounded sample: `serve_count` requests
+    simulating `serve_t_end` seconds each (the full stream is 2000 requests
+    of 2 s).  Compared with the same requests run one at a time."""
+    import threading
+
+    import ela3d_gb300 as E
+    from ela3d_gb300 import configs
+
+    reqs = [configs.serving_request(1000 + q, t_end=args.serve_t_end) for q in range(args.serve_count)]
+    work = [p.cells * p.nstep for p, *_ in reqs]
+    total = float(sum(work))
+    # the plain single-shot path: each request alone, device time of its run
+    alone_s = 0.0
+    t0 = time.perf_counter()
+    for p, cp, cs, rho in reqs:
+        with E.Plan(p, cp, cs, rho) as pl:
+            alone_s += pl.run_timed(p.nstep) / 1e3
+            pl.seismograms()
+    alone_wall = time.perf_counter() - t0
+    alone = total / alone_s / 1e9
+    rng = np.random.default_rng(7)
+    capacity = None
+    rows = []
+    for load in args.serve_loads:
+        with E.Server(steps_per_round=args.serve_round) as srv:
+            gaps = None
+            if load > 0 and capacity:
+                rate = load * capacity                       # requests per second
+                gaps = rng.exponential(1.0 / rate, len(reqs))
+            tickets = []
+
+            def client():
+                for q, r in enumerate(reqs):
+                    if gaps is not None:
+                        time.sleep(gaps[q])
+                    tickets.append(srv.submit(*r))
+
+            t_start = time.perf_counter()
+            th = threading.Thread(target=client)
+            th.start()
+            th.join()
+            for t in tickets:
+                srv.wait(t)
+            wall = time.perf_counter() - t_start
+            st = srv.stats()
+        thr = total / wall / 1e9
+        busy = total / st["busy_seconds"] / 1e9
+        if load == 0:
+            capacity = len(reqs) / wall
+        rows.append({"offered_load": "saturation" if load == 0 else load,
+                     "arrival_rate_per_s": None if load == 0 else load * capacity,
+                     "requests": len(reqs), "gcells_per_s_wall": thr, "gcells_per_s_busy": busy,
+                     "p50_latency_s": st["latency_p50_s"], "p99_latency_s": st["latency_p99_s"],
+                     "max_latency_s": st["latency_max_s"], "rounds": st["rounds"], "failed": st["failed"]})
+    sat = rows[0]
+    sizes = [p.cells for p, *_ in reqs]
+    return {"workload": f"serving stream: {len(reqs)} requests (seeded lognormal edges in [64, 384], "
+                        f"{min(sizes) / 1e6:.2f}-{max(sizes) / 1e6:.1f} Mcells, t_end {args.serve_t_end} s "
+                        f"each; the full stream is 2000 requests of 2 s), FP32",
+            "metric": METRIC, "value": sat["gcells_per_s_wall"], "p50_latency_s": sat["p50_latency_s"],
+            "p99_latency_s": sat["p99_latency_s"],
+            "single_shot_sequential_value": alone, "single_shot_sequential_wall_value": total / alone_wall / 1e9,
+            "ratio_vs_single_shot": sat["gcells_per_s_wall"] / alone,
+            "sweep": rows, "steps_per_round": args.serve_round,
+            "timing": "wall clock from first submission to last completion (requests submitted from host "
+                      "arrays, seismograms streamed back); single-shot value = device time of each request "
+                      "run alone"}
+
+
 def run_reference(args, rank, world, local):
     if rank != 0:
         return
@@ -431,6 +505,11 @@ def main():
     ap.add_argument("--batch-chunk", type=int, default=16)
     ap.add_argument("--uneven-count", type=int, default=48)
     ap.add_argument("--uneven-steps", type=int, default=100)
+    ap.add_argument("--serve-count", type=int, default=64)
+    ap.add_argument("--serve-t-end", type=float, default=0.25)
+    ap.add_argument("--serve-round", type=int, default=50)
+    ap.add_argument("--serve-loads", type=float, nargs="+", default=[0.0, 0.3, 0.6, 0.9],
+                    help="offered load as a fraction of the measured saturation rate (0 = all at once)")
     ap.add_argument("--cpu-steps", type=int, default=20)
     ap.add_argument("--ref-steps-cap", type=int, default=20)
     args = ap.parse_args()
