@@ -270,8 +270,16 @@ def run_ours(args, rank, world, local):
     dist = Dist(world, True)
     p, cp, cs, rho = workload()
     cells = p.cells
+    tune = {"variant": -1, "schedule": -1, "chunk": 0}
+    tune_info = {"source": "built-in default"}
+    if not args.no_autotune:
+        best, ms_best, cand = E.autotune([(p, cp, cs, rho)], steps=10)
+        tune = {"variant": best.variant, "schedule": best.schedule, "chunk": best.chunk}
+        v = E.variants()[best.variant]
+        tune_info = {"source": "ela3d_autotune", "candidates": cand, "tile": [v.tile_x, v.tile_y],
+                     "stages": v.stages, "schedule": best.schedule, "chunk": best.chunk}
     clocks = ClockSampler(local)
-    plan = E.Plan(p, cp, cs, rho)
+    plan = E.Plan(p, cp, cs, rho, **tune)
     plan.run(args.warmup)
     clocks.start()
     plan.set_kernel_timing(True)
@@ -291,7 +299,7 @@ def run_ours(args, rank, world, local):
     if not args.no_e2e:
         dist.barrier()
         t0 = time.perf_counter()
-        with E.Plan(p, cp, cs, rho) as shot:
+        with E.Plan(p, cp, cs, rho, **tune) as shot:
             shot.run(p.nstep)
             seis = shot.seismograms()
         t_e2e = dist.max(time.perf_counter() - t0)
@@ -336,7 +344,7 @@ def run_ours(args, rank, world, local):
                 "warmup": args.warmup, "ms_per_step": t_max * 1e3 / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32",
                 "data": "synthetic (seeded anticline model)",
-                "config": config_block(p, {"steps_timed": args.steps}),
+                "config": config_block(p, {"steps_timed": args.steps, "tuning": tune_info}),
                 "e2e": e2e, "gpu_launches": int(2 * args.steps * world), "roofline": roof,
                 "cpu_baseline": cpu, "clocks": clk}
         line.update(extra)
@@ -352,8 +360,15 @@ def batched_shots(args, single_value: float) -> dict:
 
     shots, cp, cs, rho = configs.anticline_256_shots(args.batch_shots)
     cells = sum(p.cells for p in shots)
+    tune = {"schedule": args.batch_schedule, "chunk": args.batch_chunk}
+    tune_info = {"source": "command line"}
+    if not args.no_autotune:
+        # tuned on 8 of the shots (the per-cell speed is what differs)
+        best, _, cand = E.autotune([(p, cp, cs, rho) for p in shots[:8]], steps=5)
+        tune = {"variant": best.variant, "schedule": best.schedule, "chunk": best.chunk}
+        tune_info = {"source": "ela3d_autotune on 8 of the shots", "candidates": cand, **tune}
     t0 = time.perf_counter()
-    with E.Batch([(p, cp, cs, rho) for p in shots], schedule=args.batch_schedule, chunk=args.batch_chunk) as b:
+    with E.Batch([(p, cp, cs, rho) for p in shots], **tune) as b:
         t_create = time.perf_counter() - t0
         b.run(args.warmup)
         ms = b.run_timed(args.batch_steps)
@@ -371,7 +386,7 @@ def batched_shots(args, single_value: float) -> dict:
             "ratio_vs_single_shot": value / single_value,
             "frac_of_hbm_at_142B": value * bpc / peak,
             "create_s": t_create, "readback_s": t_read,
-            "schedule": {"kind": args.batch_schedule, "chunk": args.batch_chunk},
+            "tuning": tune_info,
             "timing": "CUDA events around replayed 50-step graphs; model stored once"}
 
 
@@ -384,13 +399,20 @@ def uneven_batch(args) -> dict:
     inst = configs.uneven_batch(count=args.uneven_count)
     steps = args.uneven_steps
     cells = sum(p.cells for p, *_ in inst)
+    tune = {}
+    tune_info = {"source": "built-in default"}
+    if not args.no_autotune:
+        # tuned on every sixth instance (a cross-section of the sizes)
+        best, _, cand = E.autotune(inst[::6], steps=5)
+        tune = {"variant": best.variant, "schedule": best.schedule, "chunk": best.chunk}
+        tune_info = {"source": "ela3d_autotune on every sixth instance", "candidates": cand, **tune}
     alone_s = 0.0
     for p, cp, cs, rho in inst:
         with E.Plan(p, cp, cs, rho) as pl:
             pl.run(3)
             alone_s += pl.run_timed(steps) / 1e3
     alone = cells * steps / alone_s / 1e9
-    with E.Batch(inst) as b:
+    with E.Batch(inst, **tune) as b:
         b.run(3)
         ms = b.run_timed(steps)
     value = cells * steps / (ms / 1e3) / 1e9
@@ -398,7 +420,7 @@ def uneven_batch(args) -> dict:
     return {"workload": f"uneven_batch: {len(inst)} grids, edges from multiples of 16 in [64, 320] (seed 1), "
                         f"{min(sizes) / 1e6:.2f}-{max(sizes) / 1e6:.1f} Mcells, random 3-6 layer domes, FP32",
             "metric": METRIC, "value": value, "steps_timed": steps,
-            "single_shot_sequential_value": alone, "ratio_vs_single_shot": value / alone,
+            "single_shot_sequential_value": alone, "ratio_vs_single_shot": value / alone, "tuning": tune_info,
             "timing": "CUDA events; the same steps of every instance, batched vs one plan at a time"}
 
 
@@ -499,6 +521,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end shot (short profiling runs)")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched and uneven workloads")
+    ap.add_argument("--no-autotune", action="store_true", help="use the built-in kernel choice")
     ap.add_argument("--batch-shots", type=int, default=64)
     ap.add_argument("--batch-steps", type=int, default=100)
     ap.add_argument("--batch-schedule", type=int, default=2)

@@ -60,6 +60,8 @@ SIGNATURES = [
     ("ela3d_server_release", _c.c_int, [_P, _c.c_uint64]),
     ("ela3d_server_stats_get", _c.c_int, [_P, _P]),
     ("ela3d_server_destroy", _c.c_int, [_P]),
+    ("ela3d_autotune", _c.c_int, [_c.c_int32, _P, _P, _P, _P, _c.c_int32, _P, _c.POINTER(_c.c_double),
+                                   _c.POINTER(_c.c_int32)]),
     ("ela3d_variant_count", _c.c_int32, []),
     ("ela3d_variant_get", _c.c_int, [_c.c_int32, _P]),
     ("ela3d_plan_create_tuned", _c.c_int, [_c.POINTER(CParams), _P, _P, _P, _P, _c.POINTER(_P)]),
@@ -430,3 +432,31 @@ class Server:
             self.close()
         except Exception:
             pass
+
+
+def autotune(shots, steps: int = 10) -> tuple[Tuning, float, int]:
+    """Runs the library's autotuner on a list of (ShotParams, cp, cs, rho);
+    returns (best tuning, its ms for `steps` steps, candidates timed)."""
+    lib = load_library()
+    n = len(shots)
+    structs = (CParams * n)()
+    keep = []
+    ptrs = {k: (ctypes.c_void_p * n)() for k in ("cp", "cs", "rho")}
+    seen = {}
+    for i, (p, cp, cs, rho) in enumerate(shots):
+        c, rec = p.to_c()
+        structs[i] = c
+        keep.append(rec)
+        for key, arr in (("cp", cp), ("cs", cs), ("rho", rho)):
+            m = seen.get(id(arr))
+            if m is None:
+                m = np.ascontiguousarray(arr, dtype=np.float32).reshape(-1)
+                seen[id(arr)] = m
+                keep.append(m)
+            ptrs[key][i] = m.ctypes.data
+    best = Tuning()
+    ms = ctypes.c_double()
+    cand = ctypes.c_int32()
+    _check(lib.ela3d_autotune(n, structs, ptrs["cp"], ptrs["cs"], ptrs["rho"], steps, ctypes.byref(best),
+                              ctypes.byref(ms), ctypes.byref(cand)), "ela3d_autotune")
+    return best, ms.value, cand.value

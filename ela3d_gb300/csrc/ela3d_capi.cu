@@ -1,6 +1,8 @@
 // ela3d_capi.cu -- the extern "C" entry points of include/ela3d.h.
 #include <cmath>
+#include <cstdlib>
 #include <new>
+#include <vector>
 
 #include "ela3d_engine.h"
 
@@ -95,8 +97,27 @@ ela3d_status ela3d_variant_get(int32_t index, ela3d_variant_info *out) {
   return ELA3D_OK;
 }
 
-static TuneChoice resolve_tuning(const ela3d_params &p, const ela3d_tuning *t) {
+// The choice for a workload: fields the caller set win; the rest come from
+// the autotuner's cache (tuning on a miss when ELA3D_AUTOTUNE=1), else the
+// built-in default.
+static TuneChoice resolve_tuning(const std::vector<ela3d_params> &ps, const float *const *cp,
+                                 const float *const *cs, const float *const *rho, const ela3d_tuning *t) {
+  const ela3d_params &p = ps[0];
   TuneChoice c = default_choice(p.precision == ELA3D_FP64, p.nx, p.ny, p.nz);
+  const bool explicit_variant = t && t->variant >= 0;
+  if (!explicit_variant) {
+    TuneChoice cached{};
+    if (tune_lookup(ps, &cached)) {
+      c = cached;
+    } else {
+      const char *env = std::getenv("ELA3D_AUTOTUNE");
+      if (env && env[0] == '1' && cp && cs && rho) {
+        std::vector<const float *> a(cp, cp + ps.size()), b(cs, cs + ps.size()), r(rho, rho + ps.size());
+        TuneChoice tuned{};
+        if (autotune(ps, a, b, r, 10, &tuned, nullptr, nullptr) == ELA3D_OK) c = tuned;
+      }
+    }
+  }
   if (!t) return c;
   if (t->variant >= 0) c.variant = t->variant;
   if (t->schedule >= 0) c.kind = t->schedule;
@@ -121,7 +142,7 @@ ela3d_status ela3d_plan_create_tuned(const ela3d_params *p, const float *cp, con
   plan->p = *p;
   plan->eng = make_engine(plan->fp64, &st);
   if (st == ELA3D_OK) st = plan->eng->add_shot(*p, cp, cs, rho, -1);
-  const TuneChoice c = resolve_tuning(*p, tune);
+  const TuneChoice c = resolve_tuning({*p}, &cp, &cs, &rho, tune);
   if (st == ELA3D_OK) st = plan->eng->finalize(&c);
   if (st != ELA3D_OK) {
     delete plan;
@@ -309,7 +330,7 @@ ela3d_status ela3d_batch_create(int32_t nshots, const ela3d_params *params, cons
   }
   if (st == ELA3D_OK) {
     b->eng->set_retire(true);
-    const TuneChoice c = resolve_tuning(params[0], tune);
+    const TuneChoice c = resolve_tuning(std::vector<ela3d_params>(params, params + nshots), cp, cs, rho, tune);
     st = b->eng->finalize(&c);
   }
   if (st != ELA3D_OK) {

@@ -6,6 +6,7 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <memory>
 #include <string>
 #include <vector>
@@ -49,6 +50,14 @@ struct TuneChoice {
   int blocks_per_sm;  // 0 = occupancy limit
 };
 TuneChoice default_choice(int fp64, int nx, int ny, int nz);
+
+// Autotuner (ela3d_tune.cu): process-wide cache of measured best choices
+// keyed by the workload shape.
+bool tune_lookup(const std::vector<ela3d_params> &ps, TuneChoice *out);
+void tune_store(const std::vector<ela3d_params> &ps, const TuneChoice &c);
+ela3d_status autotune(const std::vector<ela3d_params> &ps, const std::vector<const float *> &cp,
+                      const std::vector<const float *> &cs, const std::vector<const float *> &rho, int steps,
+                      TuneChoice *best, double *best_ms, std::vector<std::pair<TuneChoice, double>> *table);
 
 class EngineBase {
  public:

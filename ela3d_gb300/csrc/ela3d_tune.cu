@@ -1,0 +1,175 @@
+// ela3d_tune.cu -- the autotuner: times every compiled kernel variant (tile
+// shape and pipeline depth) with the work schedules (z-chunk size, shot-major
+// or shot-interleaved order) on the caller's own shots and keeps the fastest
+// per workload shape.  Results live in a process-wide cache that plan and
+// batch creation consult; ELA3D_TUNE_CACHE=<file> persists it across
+// processes and ELA3D_AUTOTUNE=1 tunes on a cache miss at creation.
+#include <cstdio>
+#include <cstdlib>
+#include <map>
+#include <mutex>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "ela3d_engine.h"
+
+namespace ela3d {
+
+namespace {
+std::mutex g_mu;
+std::map<std::string, TuneChoice> g_cache;
+bool g_loaded = false;
+
+const char *cache_file() {
+  const char *f = std::getenv("ELA3D_TUNE_CACHE");
+  return (f && *f) ? f : nullptr;
+}
+
+void load_locked() {
+  if (g_loaded) return;
+  g_loaded = true;
+  const char *f = cache_file();
+  if (!f) return;
+  FILE *fp = std::fopen(f, "r");
+  if (!fp) return;
+  char key[512];
+  TuneChoice c{};
+  while (std::fscanf(fp, "%511s %d %d %d %d", key, &c.variant, &c.kind, &c.chunk, &c.blocks_per_sm) == 5)
+    g_cache[key] = c;
+  std::fclose(fp);
+}
+
+void save_locked() {
+  const char *f = cache_file();
+  if (!f) return;
+  FILE *fp = std::fopen(f, "w");
+  if (!fp) return;
+  for (auto &kv : g_cache)
+    std::fprintf(fp, "%s %d %d %d %d\n", kv.first.c_str(), kv.second.variant, kv.second.kind, kv.second.chunk,
+                 kv.second.blocks_per_sm);
+  std::fclose(fp);
+}
+}  // namespace
+
+// Workload shape: precision, shot count and the sorted set of grid sizes
+// and PML widths (what the kernels' speed depends on).
+std::string tune_key(const std::vector<ela3d_params> &ps) {
+  std::vector<std::string> parts;
+  for (auto &p : ps) {
+    std::ostringstream o;
+    o << p.nx << "x" << p.ny << "x" << p.nz << "p" << p.npml;
+    parts.push_back(o.str());
+  }
+  std::sort(parts.begin(), parts.end());
+  std::ostringstream k;
+  k << (ps.empty() ? 0 : ps[0].precision) << ":" << ps.size() << ":";
+  // many-shot keys keep the distinct shapes with counts
+  for (size_t i = 0; i < parts.size();) {
+    size_t j = i;
+    while (j < parts.size() && parts[j] == parts[i]) ++j;
+    k << parts[i] << "*" << (j - i) << ",";
+    i = j;
+  }
+  return k.str();
+}
+
+bool tune_lookup(const std::vector<ela3d_params> &ps, TuneChoice *out) {
+  std::lock_guard<std::mutex> g(g_mu);
+  load_locked();
+  auto it = g_cache.find(tune_key(ps));
+  if (it == g_cache.end()) return false;
+  *out = it->second;
+  return true;
+}
+
+void tune_store(const std::vector<ela3d_params> &ps, const TuneChoice &c) {
+  std::lock_guard<std::mutex> g(g_mu);
+  load_locked();
+  g_cache[tune_key(ps)] = c;
+  save_locked();
+}
+
+// Candidate schedules for a workload.
+static std::vector<TuneChoice> schedules(int nshots) {
+  std::vector<TuneChoice> v;
+  v.push_back({0, 0, 16, 0});
+  for (int ch : {8, 16, 32}) v.push_back({0, 1, ch, 0});
+  if (nshots > 1)
+    for (int ch : {8, 16}) v.push_back({0, 2, ch, 0});
+  return v;
+}
+
+ela3d_status autotune(const std::vector<ela3d_params> &ps, const std::vector<const float *> &cp,
+                      const std::vector<const float *> &cs, const std::vector<const float *> &rho, int steps,
+                      TuneChoice *best, double *best_ms, std::vector<std::pair<TuneChoice, double>> *table) {
+  if (ps.empty() || steps < 1) return ELA3D_ERR_INVALID_ARG;
+  const int fp64 = ps[0].precision == ELA3D_FP64;
+  int nv = 0;
+  const Variant *vs = variants(&nv);
+  double best_t = 1e300;
+  TuneChoice bc{-1, 0, 0, 0};
+  for (int v = 0; v < nv; ++v) {
+    if (vs[v].fp64 != fp64) continue;
+    for (TuneChoice c : schedules((int)ps.size())) {
+      c.variant = v;
+      ela3d_status st;
+      auto eng = make_engine(fp64, &st);
+      for (size_t q = 0; q < ps.size() && st == ELA3D_OK; ++q) {
+        int share = -1;
+        for (size_t j = 0; j < q && share < 0; ++j)
+          if (cp[j] == cp[q] && cs[j] == cs[q] && rho[j] == rho[q] && ps[j].nx == ps[q].nx &&
+              ps[j].ny == ps[q].ny && ps[j].nz == ps[q].nz)
+            share = (int)j;
+        st = eng->add_shot(ps[q], cp[q], cs[q], rho[q], share);
+      }
+      if (st == ELA3D_OK) st = eng->finalize(&c);
+      if (st == ELA3D_OK) st = eng->enqueue(2);  // warm-up
+      if (st == ELA3D_OK) st = eng->sync();
+      double ms = 0.0;
+      if (st == ELA3D_OK) st = eng->run_timed(steps, &ms);
+      if (st == ELA3D_ERR_OOM) return st;
+      if (st != ELA3D_OK) continue;  // a candidate that does not run is skipped
+      if (table) table->push_back({c, ms});
+      if (ms < best_t) {
+        best_t = ms;
+        bc = c;
+      }
+    }
+  }
+  if (bc.variant < 0) {
+    set_last_error("no kernel variant ran");
+    return ELA3D_ERR_CUDA;
+  }
+  *best = bc;
+  if (best_ms) *best_ms = best_t;
+  tune_store(ps, bc);
+  return ELA3D_OK;
+}
+
+}  // namespace ela3d
+
+using namespace ela3d;
+
+extern "C" ela3d_status ela3d_autotune(int32_t nshots, const ela3d_params *params, const float *const *cp,
+                                       const float *const *cs, const float *const *rho, int32_t steps,
+                                       ela3d_tuning *best, double *best_ms, int32_t *candidates) {
+  if (nshots < 1 || !params || !cp || !cs || !rho || !best || steps < 1) return ELA3D_ERR_INVALID_ARG;
+  std::vector<ela3d_params> ps(params, params + nshots);
+  for (auto &p : ps) {
+    ela3d_status st = validate_params(p);
+    if (st != ELA3D_OK) return st;
+    if (p.precision != ps[0].precision) return ELA3D_ERR_INVALID_ARG;
+  }
+  std::vector<const float *> a(cp, cp + nshots), b(cs, cs + nshots), c(rho, rho + nshots);
+  TuneChoice bc{};
+  std::vector<std::pair<TuneChoice, double>> table;
+  ela3d_status st = autotune(ps, a, b, c, steps, &bc, best_ms, &table);
+  if (st != ELA3D_OK) return st;
+  best->variant = bc.variant;
+  best->schedule = bc.kind;
+  best->chunk = bc.chunk;
+  best->blocks_per_sm = bc.blocks_per_sm;
+  if (candidates) *candidates = (int32_t)table.size();
+  return ELA3D_OK;
+}

@@ -189,6 +189,16 @@ typedef struct ela3d_tuning {
     int32_t blocks_per_sm;  /* cap on resident blocks per SM, 0 = occupancy limit */
 } ela3d_tuning;
 
+/* Times every compiled variant with the candidate schedules on these shots
+ * (`steps` time steps each, after a warm-up) and returns the fastest choice;
+ * it is also cached for the workload's shape, so later plans and batches of
+ * that shape use it.  ELA3D_TUNE_CACHE=<file> keeps the cache across
+ * processes; ELA3D_AUTOTUNE=1 makes plan and batch creation tune on a cache
+ * miss.  candidates (may be NULL) receives the number of choices timed.
+ * No reference counterpart. */
+ela3d_status ela3d_autotune(int32_t nshots, const ela3d_params *params, const float *const *cp,
+                            const float *const *cs, const float *const *rho, int32_t steps,
+                            ela3d_tuning *best, double *best_ms, int32_t *candidates);
 int32_t ela3d_variant_count(void);
 ela3d_status ela3d_variant_get(int32_t index, ela3d_variant_info *out);
 /* ela3d_plan_create with an explicit kernel variant and schedule. */
