@@ -50,48 +50,7 @@ def log(*a):
 
 
 # ------------------------------------------------------------------ env --
-def dist_env():
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return rank, world, local
-
-
-class Dist:
-    def __init__(self, world: int, use_cuda: bool):
-        self.world = world
-        self.pg = None
-        if world > 1:
-            import torch.distributed as dist
-
-            dist.init_process_group(backend="gloo")
-            self.pg = dist
-
-    def barrier(self):
-        if self.pg:
-            self.pg.barrier()
-
-    def max(self, v: float) -> float:
-        if not self.pg:
-            return v
-        import torch
-
-        t = torch.tensor([v], dtype=torch.float64)
-        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
-        return float(t.item())
-
-    def sum(self, v: float) -> float:
-        if not self.pg:
-            return v
-        import torch
-
-        t = torch.tensor([v], dtype=torch.float64)
-        self.pg.all_reduce(t, op=self.pg.ReduceOp.SUM)
-        return float(t.item())
-
-    def close(self):
-        if self.pg:
-            self.pg.destroy_process_group()
+from ela3d_gb300.dist import Group, env as dist_env, shard  # noqa: E402
 
 
 def cuda_sync():
@@ -267,7 +226,7 @@ def run_ours(args, rank, world, local):
     from ela3d_gb300.metrics import bytes_per_cell
 
     E.select_device(local)
-    dist = Dist(world, True)
+    dist = Group(world)
     p, cp, cs, rho = workload()
     cells = p.cells
     tune = {"variant": -1, "schedule": -1, "chunk": 0}
@@ -328,9 +287,10 @@ def run_ours(args, rank, world, local):
 
     extra = {}
     if not args.no_batched:
-        extra["batched"] = batched_shots(args, value)
-        extra["uneven"] = uneven_batch(args)
-        extra["serving"] = serving(args)
+        extra["batched"] = batched_shots(args, value)   # shots split across ranks
+        if world == 1:
+            extra["uneven"] = uneven_batch(args)
+            extra["serving"] = serving(args)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -359,6 +319,8 @@ def batched_shots(args, single_value: float) -> dict:
     from ela3d_gb300.metrics import bytes_per_cell
 
     shots, cp, cs, rho = configs.anticline_256_shots(args.batch_shots)
+    rank, world, _ = dist_env()
+    shots = shard(shots, rank, world)   # independent shots: no data-path collective
     cells = sum(p.cells for p in shots)
     tune = {"schedule": args.batch_schedule, "chunk": args.batch_chunk}
     tune_info = {"source": "command line"}
@@ -376,7 +338,8 @@ def batched_shots(args, single_value: float) -> dict:
         b.run(0)
         seis = [b.seismograms(q) for q in range(len(shots))]
         t_read = time.perf_counter() - t1
-    value = cells * args.batch_steps / (ms / 1e3) / 1e9
+    g = Group(world)
+    value = g.sum(cells) * args.batch_steps / (g.max(ms) / 1e3) / 1e9
     bpc = bytes_per_cell(256, 256, 256, 16)["step"]
     peak, _ = measured_peaks()
     return {"workload": f"anticline_256_shots: {len(shots)} shots of 256^3 sharing one model, FP32, "
