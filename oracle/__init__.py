@@ -119,9 +119,11 @@ def reference_binary(fp64: bool = False) -> str | None:
     return exe if os.path.exists(exe) else None
 
 
-def write_config(path: str, p, nsteps: int, model_prefix: str, time_from: int = 1, clean: int | None = None):
+def write_config(path: str, p, nsteps: int, model_prefix: str, time_from: int = 1, clean: int | None = None,
+                 ngatx: int = 1, ngaty: int = 1, it_output: int | None = None):
     lines = [f"nx {p.nx}", f"ny {p.ny}", f"nz {p.nz}", f"dx {int(round(p.dx))}", f"dt {p.dt!r}",
-             f"nstep {nsteps}", f"sampgat {p.sampgat}", f"it_output {1 << 30}", "ngatx 1", "ngaty 1",
+             f"nstep {nsteps}", f"sampgat {p.sampgat}", f"it_output {it_output or (1 << 30)}",
+             f"ngatx {ngatx}", f"ngaty {ngaty}",
              f"npml {p.npml}", f"npower {p.npower!r}", f"k_max {p.k_max!r}", f"alpha_max {p.alpha_max!r}",
              f"rcoef {p.rcoef!r}", f"vpml {p.vpml!r}", f"f0 {p.f0!r}", f"t0 {p.t0!r}", f"factor {p.factor!r}",
              f"angle {p.angle_force!r}", "src %d %d %d" % tuple(int(v) for v in p.src),
@@ -135,7 +137,8 @@ def write_config(path: str, p, nsteps: int, model_prefix: str, time_from: int = 
 
 
 def run_reference(p, cp, cs, rho, nsteps: int | None = None, fp64: bool = False, workdir: str | None = None,
-                  time_from: int = 1, want_fields: bool = True):
+                  time_from: int = 1, want_fields: bool = True, ngatx: int = 1, ngaty: int = 1,
+                  it_output: int | None = None):
     """Runs the patched reference program.  Returns (seis, fields, seconds of
     the timed steps, number of timed steps)."""
     exe = reference_binary(fp64)
@@ -150,7 +153,8 @@ def run_reference(p, cp, cs, rho, nsteps: int | None = None, fp64: bool = False,
     try:
         for name, a in (("cp", cp), ("cs", cs), ("rho", rho)):
             np.ascontiguousarray(a, dtype=dt).tofile(os.path.join(wd, f"m_{name}.bin"))
-        write_config(os.path.join(wd, "cfg.txt"), p, nsteps, os.path.join(wd, "m_"), time_from)
+        write_config(os.path.join(wd, "cfg.txt"), p, nsteps, os.path.join(wd, "m_"), time_from,
+                     ngatx=ngatx, ngaty=ngaty, it_output=it_output)
         subprocess.run([exe, os.path.join(wd, "cfg.txt")], cwd=wd, check=True, stdout=subprocess.DEVNULL)
         nrec = np.asarray(p.rec).reshape(-1, 3).shape[0]
         seis = np.fromfile(os.path.join(wd, "seis.bin"), dt).reshape(nrec, 3, nsteps // p.sampgat)
