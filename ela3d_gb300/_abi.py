@@ -62,6 +62,9 @@ SIGNATURES = [
     ("ela3d_server_destroy", _c.c_int, [_P]),
     ("ela3d_autotune", _c.c_int, [_c.c_int32, _P, _P, _P, _P, _c.c_int32, _P, _c.POINTER(_c.c_double),
                                    _c.POINTER(_c.c_int32)]),
+    ("ela3d_plan_create_model", _c.c_int, [_c.POINTER(CParams), _P, _P, _c.POINTER(_P)]),
+    ("ela3d_model_generate", _c.c_int, [_P, _c.c_int32, _c.c_int32, _c.c_int32, _P, _P, _P]),
+    ("ela3d_server_submit_model", _c.c_int, [_P, _c.POINTER(CParams), _P, _c.POINTER(_c.c_uint64)]),
     ("ela3d_variant_count", _c.c_int32, []),
     ("ela3d_variant_get", _c.c_int, [_c.c_int32, _P]),
     ("ela3d_plan_create_tuned", _c.c_int, [_c.POINTER(CParams), _P, _P, _P, _P, _c.POINTER(_P)]),
@@ -117,6 +120,38 @@ def schedule(nx, ny, nz, tile_x, tile_y, kind, chunk, max_blocks):
     _check(lib.ela3d_schedule_build(nx, ny, nz, tile_x, tile_y, kind, chunk, max_blocks, ctypes.byref(ni),
                                     ctypes.byref(nb), items.ctypes.data, first.ctypes.data), "ela3d_schedule_build")
     return items, first
+
+
+class ModelSpec(ctypes.Structure):
+    """ctypes mirror of ela3d_model_spec."""
+    _fields_ = [("kind", ctypes.c_int32), ("nlayers", ctypes.c_int32), ("cp", ctypes.c_double * 8),
+                ("cs_ratio", ctypes.c_double * 8), ("depth", ctypes.c_double * 8), ("dome_amp", ctypes.c_double),
+                ("dome_sigma", ctypes.c_double), ("dome_xc", ctypes.c_double), ("dome_yc", ctypes.c_double),
+                ("rho_coef", ctypes.c_double), ("rho_pow", ctypes.c_double), ("perturb", ctypes.c_double),
+                ("seed", ctypes.c_uint64), ("cp0", ctypes.c_double), ("cs0", ctypes.c_double),
+                ("rho0", ctypes.c_double)]
+
+    @classmethod
+    def from_dict(cls, d: dict) -> "ModelSpec":
+        m = cls()
+        for k, v in d.items():
+            if k in ("cp", "cs_ratio", "depth"):
+                arr = getattr(m, k)
+                for i, x in enumerate(v):
+                    arr[i] = float(x)
+            else:
+                setattr(m, k, v)
+        return m
+
+
+def generate_model(spec: dict, nx: int, ny: int, nz: int):
+    """Runs the device model generator and returns (cp, cs, rho) [nz, ny, nx]."""
+    lib = load_library()
+    out = [np.empty((nz, ny, nx), np.float32) for _ in range(3)]
+    m = ModelSpec.from_dict(spec)
+    _check(lib.ela3d_model_generate(ctypes.byref(m), nx, ny, nz, out[0].ctypes.data, out[1].ctypes.data,
+                                    out[2].ctypes.data), "ela3d_model_generate")
+    return tuple(out)
 
 
 class Ela3dError(RuntimeError):
@@ -175,6 +210,23 @@ class Plan:
         _check(lib.ela3d_plan_create_tuned(ctypes.byref(c), _ptr(models[0]), _ptr(models[1]), _ptr(models[2]),
                                            ctypes.byref(t), ctypes.byref(h)), "ela3d_plan_create")
         self._h = h
+
+    @classmethod
+    def from_model(cls, params: ShotParams, spec: dict, variant: int = -1, schedule: int = -1,
+                   chunk: int = 0) -> "Plan":
+        """A plan whose model is generated on the device (ela3d_plan_create_model)."""
+        self = cls.__new__(cls)
+        lib = load_library()
+        self._lib = lib
+        self.params = params
+        c, rec = params.to_c()
+        m = ModelSpec.from_dict(spec)
+        t = Tuning(variant, schedule, chunk, -1)
+        h = ctypes.c_void_p()
+        _check(lib.ela3d_plan_create_model(ctypes.byref(c), ctypes.byref(m), ctypes.byref(t), ctypes.byref(h)),
+               "ela3d_plan_create_model")
+        self._h = h
+        return self
 
     @property
     def handle(self) -> ctypes.c_void_p:
@@ -383,6 +435,16 @@ class Server:
         t = ctypes.c_uint64()
         _check(self._lib.ela3d_server_submit(self._h, ctypes.byref(c), m[0].ctypes.data, m[1].ctypes.data,
                                              m[2].ctypes.data, ctypes.byref(t)), "ela3d_server_submit")
+        self._params[t.value] = params
+        return t.value
+
+    def submit_model(self, params: ShotParams, spec: dict) -> int:
+        """Queues a request whose model is generated on the device at admission."""
+        c, rec = params.to_c()
+        m = ModelSpec.from_dict(spec)
+        t = ctypes.c_uint64()
+        _check(self._lib.ela3d_server_submit_model(self._h, ctypes.byref(c), ctypes.byref(m), ctypes.byref(t)),
+               "ela3d_server_submit_model")
         self._params[t.value] = params
         return t.value
 

@@ -1,6 +1,7 @@
 // ela3d_capi.cu -- the extern "C" entry points of include/ela3d.h.
 #include <cmath>
 #include <cstdlib>
+#include <cstring>
 #include <new>
 #include <vector>
 
@@ -151,6 +152,52 @@ ela3d_status ela3d_plan_create_tuned(const ela3d_params *p, const float *cp, con
   plan->p.rec = nullptr;  // the engine keeps its own copy
   *out = plan;
   return ELA3D_OK;
+}
+
+static_assert(sizeof(ela3d_model_spec) == sizeof(ModelSpec), "model spec layout");
+
+ela3d_status ela3d_plan_create_model(const ela3d_params *p, const ela3d_model_spec *model,
+                                     const ela3d_tuning *tune, ela3d_plan **out) {
+  if (!p || !model || !out) return ELA3D_ERR_INVALID_ARG;
+  *out = nullptr;
+  ela3d_status st = validate_params(*p);
+  if (st != ELA3D_OK) return st;
+  ela3d_plan *plan = new (std::nothrow) ela3d_plan();
+  if (!plan) return ELA3D_ERR_OOM;
+  plan->fp64 = p->precision == ELA3D_FP64;
+  plan->p = *p;
+  plan->eng = make_engine(plan->fp64, &st);
+  ModelSpec spec;
+  std::memcpy(&spec, model, sizeof(spec));
+  if (st == ELA3D_OK) st = plan->eng->add_shot(*p, nullptr, nullptr, nullptr, -1, &spec);
+  const TuneChoice c = resolve_tuning({*p}, nullptr, nullptr, nullptr, tune);
+  if (st == ELA3D_OK) st = plan->eng->finalize(&c);
+  if (st != ELA3D_OK) {
+    delete plan;
+    return st;
+  }
+  plan->p.rec = nullptr;
+  *out = plan;
+  return ELA3D_OK;
+}
+
+ela3d_status ela3d_model_generate(const ela3d_model_spec *model, int32_t nx, int32_t ny, int32_t nz, float *cp,
+                                  float *cs, float *rho) {
+  if (!model || nx < 1 || ny < 1 || nz < 1 || !cp || !cs || !rho) return ELA3D_ERR_INVALID_ARG;
+  ModelSpec spec;
+  std::memcpy(&spec, model, sizeof(spec));
+  const size_t n = (size_t)nx * ny * nz;
+  float *d = nullptr;
+  ela3d_status st = status_from_cuda(cudaMalloc(&d, 3 * n * sizeof(float)), "cudaMalloc");
+  if (st != ELA3D_OK) return st;
+  st = status_from_cuda(launch_model_f32(spec, nx, ny, nz, nx, d, d + n, d + 2 * n, 0), "model kernel");
+  if (st == ELA3D_OK) st = status_from_cuda(cudaDeviceSynchronize(), "model kernel");
+  if (st == ELA3D_OK) st = status_from_cuda(cudaMemcpy(cp, d, n * sizeof(float), cudaMemcpyDeviceToHost), "copy");
+  if (st == ELA3D_OK) st = status_from_cuda(cudaMemcpy(cs, d + n, n * sizeof(float), cudaMemcpyDeviceToHost), "copy");
+  if (st == ELA3D_OK)
+    st = status_from_cuda(cudaMemcpy(rho, d + 2 * n, n * sizeof(float), cudaMemcpyDeviceToHost), "copy");
+  cudaFree(d);
+  return st;
 }
 
 ela3d_status ela3d_plan_create(const ela3d_params *p, const float *cp, const float *cs, const float *rho,

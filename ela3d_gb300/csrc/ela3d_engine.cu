@@ -199,6 +199,10 @@ struct Shot {
 
 template <typename T> struct Fp;
 template <> struct Fp<float> {
+  static cudaError_t model(const ModelSpec &m, int nx, int ny, int nz, int px, float *a, float *b, float *c,
+                           cudaStream_t s) {
+    return launch_model_f32(m, nx, ny, nz, px, a, b, c, s);
+  }
   static cudaError_t profile(const AxisProfileArgs &a, float *o, cudaStream_t s) { return launch_profile_f32(a, o, s); }
   static cudaError_t stf(const StfArgs &a, float *o, cudaStream_t s) { return launch_stf_f32(a, o, s); }
   static cudaError_t pad(const float *src, float *dst, int nx, int ny, int nz, int px, cudaStream_t s) {
@@ -212,6 +216,10 @@ template <> struct Fp<float> {
   }
 };
 template <> struct Fp<double> {
+  static cudaError_t model(const ModelSpec &m, int nx, int ny, int nz, int px, double *a, double *b, double *c,
+                           cudaStream_t s) {
+    return launch_model_f64(m, nx, ny, nz, px, a, b, c, s);
+  }
   static cudaError_t profile(const AxisProfileArgs &a, double *o, cudaStream_t s) { return launch_profile_f64(a, o, s); }
   static cudaError_t stf(const StfArgs &a, double *o, cudaStream_t s) { return launch_stf_f64(a, o, s); }
   static cudaError_t pad(const float *src, double *dst, int nx, int ny, int nz, int px, cudaStream_t s) {
@@ -250,7 +258,7 @@ class Engine final : public EngineBase {
   cudaStream_t stream() const override { return stream_; }
 
   ela3d_status add_shot(const ela3d_params &p, const float *cp, const float *cs, const float *rho,
-                        int shared_model_of) override {
+                        int shared_model_of, const ModelSpec *spec = nullptr) override {
     ela3d_status st = validate_params(p);
     if (st != ELA3D_OK) return st;
     if ((p.precision == ELA3D_FP64) != (sizeof(T) == 8)) BAD("precision does not match the engine");
@@ -259,9 +267,12 @@ class Engine final : public EngineBase {
       const ela3d_params &q = shots_[shared_model_of]->p;
       if (q.nx != p.nx || q.ny != p.ny || q.nz != p.nz) BAD("shared model needs equal grids");
       while (shots_[shared_model_of]->model_of >= 0) shared_model_of = shots_[shared_model_of]->model_of;
-    } else if (!cp || !cs || !rho) {
+    } else if (!spec && (!cp || !cs || !rho)) {
       BAD("model arrays missing");
     }
+    if (spec && (spec->kind < 0 || spec->kind > MODEL_MATLAB_ANTICLINE ||
+                 (spec->kind == MODEL_LAYERED_DOME && (spec->nlayers < 1 || spec->nlayers > kMaxLayers))))
+      BAD("bad model spec");
     auto sh = std::make_unique<Shot<T>>();
     Shot<T> &s = *sh;
     s.p = p;
@@ -384,8 +395,11 @@ class Engine final : public EngineBase {
     d.rec_sorted = reinterpret_cast<int4 *>(s.pool + o_rs);
     d.seis = reinterpret_cast<T *>(s.pool + o_seis);
 
-    // 3. model upload into the padded layout
-    if (shared_model_of < 0) {
+    // 3. model: generated on the device, or uploaded into the padded layout
+    if (shared_model_of < 0 && spec) {
+      T *dst[3] = {const_cast<T *>(d.cp), const_cast<T *>(d.cs), const_cast<T *>(d.rho)};
+      CK(Fp<T>::model(*spec, nx, ny, nz, px, dst[0], dst[1], dst[2], stream_));
+    } else if (shared_model_of < 0) {
       const float *src[3] = {cp, cs, rho};
       T *dst[3] = {const_cast<T *>(d.cp), const_cast<T *>(d.cs), const_cast<T *>(d.rho)};
       if (sizeof(T) == 4) {

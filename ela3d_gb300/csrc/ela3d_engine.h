@@ -62,8 +62,10 @@ ela3d_status autotune(const std::vector<ela3d_params> &ps, const std::vector<con
 class EngineBase {
  public:
   virtual ~EngineBase() = default;
+  // The model comes from host arrays (cp, cs, rho), from another shot
+  // (shared_model_of >= 0), or from a generator run on the device (spec).
   virtual ela3d_status add_shot(const ela3d_params &p, const float *cp, const float *cs, const float *rho,
-                                int shared_model_of) = 0;
+                                int shared_model_of, const ModelSpec *spec = nullptr) = 0;
   virtual ela3d_status finalize(const TuneChoice *choice) = 0;
   virtual ela3d_status enqueue(int nsteps) = 0;
   // enqueue bracketed by events on the engine's stream; waits, returns ms

@@ -60,4 +60,20 @@ cudaError_t launch_tick_add(int *dtick, int delta, cudaStream_t s);
 cudaError_t launch_energy_f32(const ShotDesc<float> *shot, int nx, int ny, int nz, double *out, cudaStream_t s);
 cudaError_t launch_energy_f64(const ShotDesc<double> *shot, int nx, int ny, int nz, double *out, cudaStream_t s);
 
+// Model generated on the device (ela3d_media.cu); mirrors ela3d_model_spec.
+enum { MODEL_HOMOGENEOUS = 0, MODEL_LAYERED_DOME = 1, MODEL_MATLAB_ANTICLINE = 2 };
+constexpr int kMaxLayers = 8;
+struct ModelSpec {
+  int kind, nlayers;
+  double cp[kMaxLayers], cs_ratio[kMaxLayers], depth[kMaxLayers];
+  double dome_amp, dome_sigma, dome_xc, dome_yc;
+  double rho_coef, rho_pow, perturb;
+  unsigned long long seed;
+  double cp0, cs0, rho0;
+};
+cudaError_t launch_model_f32(const ModelSpec &s, int nx, int ny, int nz, int px, float *cp, float *cs, float *rho,
+                             cudaStream_t st);
+cudaError_t launch_model_f64(const ModelSpec &s, int nx, int ny, int nz, int px, double *cp, double *cs,
+                             double *rho, cudaStream_t st);
+
 }  // namespace ela3d

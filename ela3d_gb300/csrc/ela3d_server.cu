@@ -44,6 +44,8 @@ struct Request {
   ela3d_params p{};
   std::vector<int32_t> rec;
   std::vector<float> cp, cs, rho;  // host copies until admitted
+  bool generated = false;          // model generated on the device instead
+  ModelSpec spec{};
   int64_t footprint = 0;
   int state = RQ_QUEUED;
   ela3d_status error = ELA3D_OK;
@@ -130,7 +132,8 @@ struct ela3d_server {
       for (Request *r : admit) {
         ela3d_params p = r->p;
         p.rec = r->rec.data();
-        ela3d_status st = eng->add_shot(p, r->cp.data(), r->cs.data(), r->rho.data(), -1);
+        ela3d_status st = r->generated ? eng->add_shot(p, nullptr, nullptr, nullptr, -1, &r->spec)
+                                       : eng->add_shot(p, r->cp.data(), r->cs.data(), r->rho.data(), -1);
         admitted.push_back({r, st});
         if (st == ELA3D_OK) r->key = eng->last_key();
       }
@@ -269,6 +272,41 @@ ela3d_status ela3d_server_create(const ela3d_server_config *cfg, ela3d_server **
   return ELA3D_OK;
 }
 
+static ela3d_status submit_common(ela3d_server *s, std::unique_ptr<Request> r, uint64_t *ticket) {
+  std::lock_guard<std::mutex> g(s->mu);
+  if (s->fatal != ELA3D_OK) return s->fatal;
+  r->ticket = s->next_ticket++;
+  if (s->n_submitted == 0) s->t_first = r->t_submit;
+  ++s->n_submitted;
+  *ticket = r->ticket;
+  s->queue.push_back(r->ticket);
+  s->reqs[r->ticket] = std::move(r);
+  s->cv_work.notify_all();
+  return ELA3D_OK;
+}
+
+ela3d_status ela3d_server_submit_model(ela3d_server *s, const ela3d_params *p, const ela3d_model_spec *model,
+                                       uint64_t *ticket) {
+  if (!s || !p || !model || !ticket) return ELA3D_ERR_INVALID_ARG;
+  ela3d_status st = validate_params(*p);
+  if (st != ELA3D_OK) return st;
+  if (p->precision != s->cfg.precision) {
+    set_last_error("request precision differs from the server's");
+    return ELA3D_ERR_INVALID_ARG;
+  }
+  auto r = std::make_unique<Request>();
+  r->p = *p;
+  r->rec.assign(p->rec, p->rec + 3 * (size_t)p->nrec);
+  r->p.rec = nullptr;
+  r->generated = true;
+  std::memcpy(&r->spec, model, sizeof(ModelSpec));
+  r->footprint = s->eng->footprint(*p);
+  r->nsamp = p->nstep / p->sampgat;
+  r->seis.assign((size_t)p->nrec * 3 * r->nsamp, 0.0f);
+  r->t_submit = now_s();
+  return submit_common(s, std::move(r), ticket);
+}
+
 ela3d_status ela3d_server_submit(ela3d_server *s, const ela3d_params *p, const float *cp, const float *cs,
                                  const float *rho, uint64_t *ticket) {
   if (!s || !p || !ticket) return ELA3D_ERR_INVALID_ARG;
@@ -294,16 +332,7 @@ ela3d_status ela3d_server_submit(ela3d_server *s, const ela3d_params *p, const f
   r->nsamp = p->nstep / p->sampgat;
   r->seis.assign((size_t)p->nrec * 3 * r->nsamp, 0.0f);
   r->t_submit = now_s();
-  std::lock_guard<std::mutex> g(s->mu);
-  if (s->fatal != ELA3D_OK) return s->fatal;
-  r->ticket = s->next_ticket++;
-  if (s->n_submitted == 0) s->t_first = r->t_submit;
-  ++s->n_submitted;
-  *ticket = r->ticket;
-  s->queue.push_back(r->ticket);
-  s->reqs[r->ticket] = std::move(r);
-  s->cv_work.notify_all();
-  return ELA3D_OK;
+  return submit_common(s, std::move(r), ticket);
 }
 
 ela3d_status ela3d_server_poll(ela3d_server *s, uint64_t ticket, int32_t *state, int32_t *samples_ready) {

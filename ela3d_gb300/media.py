@@ -94,3 +94,90 @@ def random_anticline(rng: np.random.Generator, nx: int, ny: int, nz: int, cp_ran
     cs = cp / ratios[layer]
     rho = 310.0 * cp ** 0.25
     return cp.astype(np.float32), cs.astype(np.float32), rho.astype(np.float32)
+
+
+# ---------------------------------------------------------------------------
+# Models generated on the GPU (ela3d_model_spec in include/ela3d.h).  The
+# functions below build the specs; ``generate_host`` is a host restatement
+# of the device generator used to check it.
+MODEL_HOMOGENEOUS, MODEL_LAYERED_DOME, MODEL_MATLAB_ANTICLINE = 0, 1, 2
+
+
+def homogeneous_spec(cp: float, cs: float, rho: float) -> dict:
+    return {"kind": MODEL_HOMOGENEOUS, "cp0": cp, "cs0": cs, "rho0": rho}
+
+
+def dome_spec(nx: int, ny: int, depths, cps, cs_ratio, amp: float, sigma: float, rho_coef: float = 310.0,
+              rho_pow: float = 0.25, perturb: float = 0.0, seed: int = 0, xc=None, yc=None) -> dict:
+    """Layered dome: layer L below interface L-1; cs_ratio per layer (a
+    number applies to all)."""
+    n = len(cps)
+    ratios = [cs_ratio] * n if np.isscalar(cs_ratio) else list(cs_ratio)
+    return {"kind": MODEL_LAYERED_DOME, "nlayers": n, "cp": list(cps), "cs_ratio": ratios,
+            "depth": list(depths)[:n], "dome_amp": amp, "dome_sigma": sigma,
+            "dome_xc": (nx - 1) / 2.0 if xc is None else xc, "dome_yc": (ny - 1) / 2.0 if yc is None else yc,
+            "rho_coef": rho_coef, "rho_pow": rho_pow, "perturb": perturb, "seed": seed}
+
+
+def matlab_spec() -> dict:
+    return {"kind": MODEL_MATLAB_ANTICLINE}
+
+
+def anticline_256_spec(n: int = 256, seed: int = 0) -> dict:
+    """The 256^3 four-layer dome of configs.anticline_256 with the device's
+    hash noise (same statistics as the host model, a different realisation)."""
+    s = n / 256.0
+    return dome_spec(n, n, [d * s for d in (40, 90, 150, 210)], [2000.0, 2800.0, 3500.0, 4200.0], 1.73,
+                     25.0 * s, 50.0 * s, perturb=0.02, seed=seed)
+
+
+def _splitmix_uniform(seed: int, cell: np.ndarray, stream: int) -> np.ndarray:
+    with np.errstate(over="ignore"):
+        z = (np.uint64(seed) + np.uint64(0x9E3779B97F4A7C15) * (cell.astype(np.uint64) * np.uint64(2)
+                                                                 + np.uint64(stream + 1)))
+        z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+        z = z ^ (z >> np.uint64(31))
+    return (z >> np.uint64(11)).astype(np.float64) * (1.0 / 9007199254740992.0)
+
+
+def generate_host(spec: dict, nx: int, ny: int, nz: int):
+    """Host restatement of the device generator (float32 [nz, ny, nx])."""
+    kind = spec["kind"]
+    shape = (nz, ny, nx)
+    if kind == MODEL_HOMOGENEOUS:
+        return tuple(np.full(shape, np.float32(spec[k]), np.float32) for k in ("cp0", "cs0", "rho0"))
+    k = np.arange(nz, dtype=np.float64)[:, None, None]
+    y = np.arange(ny, dtype=np.float64)[None, :, None]
+    x = np.arange(nx, dtype=np.float64)[None, None, :]
+    if kind == MODEL_LAYERED_DOME:
+        dome = spec["dome_amp"] * np.exp(-((x - spec["dome_xc"]) ** 2 + (y - spec["dome_yc"]) ** 2)
+                                         / (2.0 * spec["dome_sigma"] ** 2))
+        L = np.zeros(shape, np.int64)
+        for d in spec["depth"][: spec["nlayers"]]:
+            L += (k >= d - dome)
+        L = np.minimum(L, spec["nlayers"] - 1)
+        cpl = np.asarray(spec["cp"], np.float64)[L]
+        cs = cpl / np.asarray(spec["cs_ratio"], np.float64)[L]
+        rho = spec["rho_coef"] * cpl ** spec["rho_pow"]
+        cp = cpl.copy()
+        if spec["perturb"] > 0:
+            cell = np.arange(nx * ny * nz, dtype=np.uint64).reshape(shape)
+            cp *= 1.0 + spec["perturb"] * (2.0 * _splitmix_uniform(spec["seed"], cell, 0) - 1.0)
+            rho *= 1.0 + spec["perturb"] * (2.0 * _splitmix_uniform(spec["seed"], cell, 1) - 1.0)
+        return cp.astype(np.float32), cs.astype(np.float32), rho.astype(np.float32)
+    # MATLAB anticline, depths scaled by nz / 201
+    X = math.pi * x / (nx - 1)
+    Y = math.pi * y / (ny - 1)
+    Z = np.maximum(((np.sin(X) + np.sin(Y)) / 2.0 - 0.5) / 0.5, 0.0)
+    sc = nz / 201.0
+    kk = k + 1
+    m = np.ones(np.broadcast_shapes(kk.shape, Z.shape), np.int32)
+    m[np.broadcast_to(kk > 121 * sc - 100 * sc * Z, m.shape)] = 2
+    m3 = np.broadcast_to(kk > 161 * sc - 100 * sc * Z, m.shape)
+    m[m3] = 3
+    m[m3 & np.broadcast_to(kk < 80 * sc, m.shape)] = 4
+    m[np.broadcast_to(kk > 201 * sc - 100 * sc * Z, m.shape)] = 5
+    media = np.array([[0, 0, 0], [3000, 1700, 2800], [3600, 1400, 2300], [3000, 1700, 2800],
+                      [3600, 1700, 2800], [3650, 1500, 2450]], np.float32)
+    return media[m, 0], media[m, 1], media[m, 2]

@@ -205,6 +205,37 @@ ela3d_status ela3d_variant_get(int32_t index, ela3d_variant_info *out);
 ela3d_status ela3d_plan_create_tuned(const ela3d_params *p, const float *cp, const float *cs,
                                      const float *rho, const ela3d_tuning *tune, ela3d_plan **out);
 
+/* ---- earth models generated on the device -------------------------------- */
+/* Instead of host arrays, a plan or server request may name a model to be
+ * generated by a GPU kernel directly in its device arrays (no host arrays,
+ * no upload):
+ *  HOMOGENEOUS     cp0, cs0, rho0 everywhere (simpelmodel.cpp:45-59);
+ *  LAYERED_DOME    nlayers layers bounded by interfaces
+ *                  depth[i] - dome_amp exp(-r^2 / (2 dome_sigma^2)) (cells,
+ *                  r from (dome_xc, dome_yc)); cs = cp / cs_ratio[L],
+ *                  rho = rho_coef cp^rho_pow; cp and rho get independent
+ *                  uniform +-perturb relative noise from a counter-based hash
+ *                  of (seed, cell);
+ *  MATLAB_ANTICLINE the five-medium anticline of generate_3d_model_anticline.m
+ *                  (exactly that model at 201^3; depths scale with nz/201).
+ * Values are rounded to float32 (the model's precision) in every plan type. */
+enum { ELA3D_MODEL_HOMOGENEOUS = 0, ELA3D_MODEL_LAYERED_DOME = 1, ELA3D_MODEL_MATLAB_ANTICLINE = 2 };
+typedef struct ela3d_model_spec {
+    int32_t kind, nlayers;
+    double cp[8], cs_ratio[8], depth[8];
+    double dome_amp, dome_sigma, dome_xc, dome_yc;
+    double rho_coef, rho_pow, perturb;
+    uint64_t seed;
+    double cp0, cs0, rho0;
+} ela3d_model_spec;
+/* ela3d_plan_create with a generated model. */
+ela3d_status ela3d_plan_create_model(const ela3d_params *p, const ela3d_model_spec *model,
+                                     const ela3d_tuning *tune, ela3d_plan **out);
+/* The generated model as host arrays (nx*ny*nz float32 each), for
+ * inspection or for other tools. */
+ela3d_status ela3d_model_generate(const ela3d_model_spec *model, int32_t nx, int32_t ny, int32_t nz,
+                                  float *cp, float *cs, float *rho);
+
 /* ---- batches of shots ---------------------------------------------------- */
 /* Many shots resident together and advanced by the same two launches per
  * time step (the persistent kernels deal (shot, tile, z-run) items to all
@@ -266,6 +297,9 @@ ela3d_status ela3d_server_submit(ela3d_server *s, const ela3d_params *p, const f
                                  const float *rho, uint64_t *ticket);
 /* State and number of seismogram samples available so far. */
 ela3d_status ela3d_server_poll(ela3d_server *s, uint64_t ticket, int32_t *state, int32_t *samples_ready);
+/* ela3d_server_submit with a model generated on the device at admission. */
+ela3d_status ela3d_server_submit_model(ela3d_server *s, const ela3d_params *p, const ela3d_model_spec *model,
+                                       uint64_t *ticket);
 /* Samples [first, first+count) of every trace, [nrec][3][count]; returns
  * ELA3D_ERR_NOT_READY if they have not all arrived. */
 ela3d_status ela3d_server_read(ela3d_server *s, uint64_t ticket, int32_t first, int32_t count, float *out);

@@ -150,3 +150,23 @@ def test_plan_without_gpu_fails_loudly(built):
     m = np.ones(p.cells, np.float32)
     with pytest.raises(Ela3dError):
         Plan(p, m * 3000, m * 1700, m * 2000)
+
+
+def test_model_spec_layout_matches_header(built):
+    import ctypes as C
+    from ela3d_gb300._abi import ModelSpec
+
+    prog = r'''
+#include <stdio.h>
+#include <stddef.h>
+#include "ela3d.h"
+int main(void) { printf("%zu %zu %zu\n", sizeof(ela3d_model_spec), offsetof(ela3d_model_spec, seed),
+                        offsetof(ela3d_model_spec, rho0)); return 0; }
+'''
+    with tempfile.TemporaryDirectory() as d:
+        c = os.path.join(d, "m.c")
+        open(c, "w").write(prog)
+        subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), c, "-o", os.path.join(d, "m")], check=True)
+        size, seed, rho0 = (int(v) for v in subprocess.run([os.path.join(d, "m")], capture_output=True, text=True,
+                                                            check=True).stdout.split())
+    assert size == C.sizeof(ModelSpec) and seed == ModelSpec.seed.offset and rho0 == ModelSpec.rho0.offset
