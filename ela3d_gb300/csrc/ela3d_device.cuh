@@ -37,7 +37,10 @@ constexpr unsigned long long kTestWaitLimitNs = 20000000ull;
 // loads, so every consumer wait expires and the kernel returns
 // DEV_ERR_TIMEOUT: the failure path of a lost transfer, exercised without a
 // fault (the waits are bounded, nothing spins forever).
-enum : int { CTL_WITHHOLD_LOADS = 1 };
+// CTL_PF_X lets the producer warp prefetch into L1 the C-PML memory
+// variables of the x slab, CTL_PF_YZ those of the y and z slabs into L2
+// (performance hints; results do not depend on them).
+enum : int { CTL_WITHHOLD_LOADS = 1, CTL_PF_X = 2, CTL_PF_YZ = 4 };
 
 // Which psi variable of an axis.  Stress half-step: S0..S2, velocity: V0..V2.
 //  x: S0 dvx_dx(half) S1 dvy_dx S2 dvz_dx | V0 dsxx_dx V1 dsxy_dx(half) V2 dsxz_dx(half)
@@ -155,7 +158,7 @@ __device__ __forceinline__ void prefetch_tensormap(const CUtensorMap *map) {
   asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(map)) : "memory");
 }
 
-// 16-byte vector of T.
+// 16-byte vector of T (the TMA x granule).
 template <typename T> struct Vec;
 template <> struct Vec<float> {
   static constexpr int N = 4;
@@ -166,51 +169,59 @@ template <> struct Vec<double> {
   using V = double2;
 };
 
-template <typename T>
-__device__ __forceinline__ void ld_vec(const T *p, T (&o)[Vec<T>::N]) {
-  using V = typename Vec<T>::V;
-  V v = *reinterpret_cast<const V *>(p);
-  if constexpr (Vec<T>::N == 4) {
+// N consecutive T as one load/store (N * sizeof(T) = 4 .. 16 bytes).
+template <typename T, int N> struct VType;
+template <> struct VType<float, 4> { using V = float4; };
+template <> struct VType<float, 2> { using V = float2; };
+template <> struct VType<float, 1> { using V = float; };
+template <> struct VType<double, 2> { using V = double2; };
+template <> struct VType<double, 1> { using V = double; };
+
+template <typename T, int N>
+__device__ __forceinline__ void unpack(const typename VType<T, N>::V &v, T (&o)[N]) {
+  if constexpr (N == 4) {
     o[0] = v.x; o[1] = v.y; o[2] = v.z; o[3] = v.w;
-  } else {
+  } else if constexpr (N == 2) {
     o[0] = v.x; o[1] = v.y;
+  } else {
+    o[0] = v;
   }
 }
 
-template <typename T>
-__device__ __forceinline__ void ld_vec_global(const T *p, T (&o)[Vec<T>::N]) {
-  using V = typename Vec<T>::V;
-  V v = __ldg(reinterpret_cast<const V *>(p));
-  if constexpr (Vec<T>::N == 4) {
-    o[0] = v.x; o[1] = v.y; o[2] = v.z; o[3] = v.w;
-  } else {
-    o[0] = v.x; o[1] = v.y;
-  }
-}
-
-// Plain (coherent) 16-byte load, for data written by earlier kernels of the
-// same stream that this kernel may also write (psi).
-template <typename T>
-__device__ __forceinline__ void ld_vec_rw(const T *p, T (&o)[Vec<T>::N]) {
-  using V = typename Vec<T>::V;
-  V v = *reinterpret_cast<const V *>(p);
-  if constexpr (Vec<T>::N == 4) {
-    o[0] = v.x; o[1] = v.y; o[2] = v.z; o[3] = v.w;
-  } else {
-    o[0] = v.x; o[1] = v.y;
-  }
-}
-
-template <typename T>
-__device__ __forceinline__ void st_vec(T *p, const T (&o)[Vec<T>::N]) {
-  using V = typename Vec<T>::V;
-  V v;
-  if constexpr (Vec<T>::N == 4) {
+template <typename T, int N>
+__device__ __forceinline__ typename VType<T, N>::V pack(const T (&o)[N]) {
+  typename VType<T, N>::V v;
+  if constexpr (N == 4) {
     v.x = o[0]; v.y = o[1]; v.z = o[2]; v.w = o[3];
-  } else {
+  } else if constexpr (N == 2) {
     v.x = o[0]; v.y = o[1];
+  } else {
+    v = o[0];
   }
-  *reinterpret_cast<V *>(p) = v;
+  return v;
+}
+
+template <typename T, int N>
+__device__ __forceinline__ void ld_vec(const T *p, T (&o)[N]) {
+  unpack<T, N>(*reinterpret_cast<const typename VType<T, N>::V *>(p), o);
+}
+
+// read-only path (profiles)
+template <typename T, int N>
+__device__ __forceinline__ void ld_vec_global(const T *p, T (&o)[N]) {
+  unpack<T, N>(__ldg(reinterpret_cast<const typename VType<T, N>::V *>(p)), o);
+}
+
+// Plain (coherent) load, for data written by earlier kernels of the same
+// stream that this kernel may also write (psi).
+template <typename T, int N>
+__device__ __forceinline__ void ld_vec_rw(const T *p, T (&o)[N]) {
+  unpack<T, N>(*reinterpret_cast<const typename VType<T, N>::V *>(p), o);
+}
+
+template <typename T, int N>
+__device__ __forceinline__ void st_vec(T *p, const T (&o)[N]) {
+  *reinterpret_cast<typename VType<T, N>::V *>(p) = pack<T, N>(o);
 }
 
 }  // namespace ela3d

@@ -7,6 +7,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <numeric>
@@ -250,6 +251,7 @@ class Engine final : public EngineBase {
     CK(cudaMalloc(&d_energy_, sizeof(double)));
     CK(cudaMalloc(&d_tick_, sizeof(int)));
     CK(cudaMemset(d_tick_, 0, sizeof(int)));
+    if (const char *e = std::getenv("ELA3D_PSI_PREFETCH")) prefetch_ = std::atoi(e) & (CTL_PF_X | CTL_PF_YZ);
     return ELA3D_OK;
   }
 
@@ -573,7 +575,7 @@ class Engine final : public EngineBase {
   void set_retire(bool on) override { retire_ = on; }
 
   ela3d_status launch_step(int tick, const int *dtick) {
-    int ctl = inject_ > 0 ? CTL_WITHHOLD_LOADS : 0;
+    int ctl = (inject_ > 0 ? CTL_WITHHOLD_LOADS : 0) | prefetch_;
     if (inject_ > 0) --inject_;
     void *args[] = {&d_desc_, &d_maps_, &d_items_, &d_ranges_, &tick, &dtick, &d_err_, &ctl};
     cudaEvent_t e0 = nullptr, e1 = nullptr, e2 = nullptr;
@@ -980,6 +982,7 @@ class Engine final : public EngineBase {
   bool sched_valid_ = false, retire_ = false;
   int tick_ = 0;
   int inject_ = 0;   // steps left whose launches withhold their loads (test hook)
+  int prefetch_ = CTL_PF_X | CTL_PF_YZ;  // memory-variable prefetch hints (x slab to L1, y/z slabs to L2)
   int *d_tick_ = nullptr;
   cudaGraphExec_t gexec_ = nullptr;
   bool use_graphs_ = true, capturing_ = false;

@@ -7,9 +7,9 @@
 
 namespace ela3d {
 
-template <typename T, int TX, int TY, int NS>
+template <typename T, int TX, int TY, int NS, int CPT = Vec<T>::N, int MB = 0>
 static Variant make_variant() {
-  using G = Geo<T, TX, TY, NS>;
+  using G = Geo<T, TX, TY, NS, CPT, MB>;
   Variant v;
   v.fp64 = sizeof(T) == 8;
   v.tx = TX;
@@ -19,8 +19,8 @@ static Variant make_variant() {
   v.stress_smem = G::S_SMEM;
   v.vel_smem = G::V_SMEM;
   v.halo = G::H;
-  v.stress = reinterpret_cast<const void *>(&stress_kernel<T, TX, TY, NS>);
-  v.velocity = reinterpret_cast<const void *>(&velocity_kernel<T, TX, TY, NS>);
+  v.stress = reinterpret_cast<const void *>(&stress_kernel<T, TX, TY, NS, CPT, MB>);
+  v.velocity = reinterpret_cast<const void *>(&velocity_kernel<T, TX, TY, NS, CPT, MB>);
   return v;
 }
 

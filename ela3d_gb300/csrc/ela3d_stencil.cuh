@@ -23,24 +23,27 @@
 // threads return.
 #pragma once
 
+#include <type_traits>
+
 #include "ela3d_device.cuh"
 
 namespace ela3d {
 
-template <typename T, int TX_, int TY_, int NS_>
+template <typename T, int TX_, int TY_, int NS_, int CPT_ = Vec<T>::N, int MINB_ = 0>
 struct Geo {
-  static constexpr int VEC = Vec<T>::N;  // cells per thread (16 bytes)
-  static constexpr int H = VEC;          // halo width in x (16 bytes, the TMA x alignment)
+  static constexpr int VEC = CPT_;       // cells per thread (consecutive in x)
+  static constexpr int H = Vec<T>::N;    // halo width in x (16 bytes, the TMA x alignment)
   static constexpr int TX = TX_, TY = TY_, NS = NS_;
   static constexpr int NTX = TX / VEC;
   static constexpr int NT = NTX * TY;      // consumer threads
   static constexpr int NCW = NT / 32;      // consumer warps
   static constexpr int THREADS = NT + 32;  // + one producer warp
-  // blocks per SM the register budget is sized for: two blocks of four warps
-  // keep 255 registers per thread (64K registers, 16K per SM sub-partition)
-  static constexpr int MINB = THREADS <= 128 ? 2 : 1;
+  // blocks per SM the register budget is sized for (64K registers per SM):
+  // two blocks of four warps keep 255 registers per thread; fewer cells per
+  // thread trade registers for resident warps
+  static constexpr int MINB = MINB_ ? MINB_ : (THREADS <= 128 ? 2 : 1);
   static constexpr int WW = TX + H;
-  static_assert(TX % VEC == 0 && TX + H <= 256 && TY + 1 <= 256, "tile shape");
+  static_assert(H % VEC == 0 && TX % H == 0 && TX + H <= 256 && TY + 1 <= 256, "tile shape");
   static_assert(NT % 32 == 0, "consumer threads must fill whole warps");
   __host__ __device__ static constexpr int al(int b) { return (b + 127) & ~127; }
   static constexpr int C = TX * TY;          // center box
@@ -90,28 +93,100 @@ __device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 
-// Producer: one thread walks the block's items and issues every plane's
-// loads.  Load n goes to stage n % NS; before reusing a stage it waits for
-// the consumers' release of load n - NS on that stage's empty barrier.
-// Item i contributes planes k0 .. k1 (k1 is the look-ahead plane, possibly
-// nz, which the TMA fills with zeros).
-template <int NS, typename Issue>
+// L1 prefetch of every 128-byte line of [p, p + bytes).
+__device__ __forceinline__ void prefetch_l1(const void *p, int bytes) {
+  const uintptr_t a = reinterpret_cast<uintptr_t>(p);
+  for (uintptr_t q = a & ~uintptr_t(127); q < a + (uintptr_t)bytes; q += 128)
+    asm volatile("prefetch.global.L1 [%0];" ::"l"(q));
+}
+
+// L1 prefetch of the x-slab C-PML memory variables var0 .. var0+2 that the
+// consumers of a tile will load: every row of the tile crosses the x slab
+// at the tile's edge columns, so without it every consumer warp waits on
+// DRAM once per plane.  Issued by the producer warp's lanes (one (variable,
+// row) pair per lane) when a plane's stage is requested, NS-2 planes ahead
+// of the consumers.  A hint: no result depends on it.  (Prefetching the y
+// and z slabs into L1 the same way measured slower: whole warps load those
+// rows and planes, and the extra lines crowd L1.)
+// The y- and z-slab rows are brought into L2 instead (CTL_PF_YZ), with bulk
+// prefetches that need no L1 space.
+__device__ __forceinline__ void prefetch_l2_bulk(const void *p, int bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
+}
+
+template <typename T, int TX, int TY>
+struct PsiPrefetch {
+  const T *left = nullptr, *right = nullptr;  // this lane's x-slab segments at plane 0
+  const T *yrow = nullptr, *zrow = nullptr;   // this lane's y-slab row at plane 0, z-slab row at slab plane 0
+  int lbytes = 0, rbytes = 0, wbytes = 0;
+  long long pstride = 0, ystride = 0, zstride = 0;  // elements per plane of the x, y and z slabs
+  int nz = 0, zl = 0, zr = 0;
+  __device__ __forceinline__ void begin(const ShotDesc<T> &sd, int x0, int y0, int var0, int lane, int ctl) {
+    const int rows = min(TY, sd.ny - y0);
+    lbytes = rbytes = wbytes = 0;
+    yrow = zrow = nullptr;
+    nz = sd.nz;
+    zl = sd.zl;
+    zr = sd.zr;
+    pstride = (long long)sd.ny * sd.xw;
+    ystride = (long long)sd.yw * sd.px;
+    zstride = (long long)sd.ny * sd.px;
+    if (lane >= 3 * rows) return;
+    const int var = var0 + lane / rows, y = y0 + lane % rows;
+    if (ctl & CTL_PF_X) {
+      const T *row = sd.psi_x + var * sd.psx + (long long)y * sd.xw;
+      const int xb = min(x0 + TX, sd.xl);
+      const int xc = max(x0, sd.xr), xd = min(x0 + TX, sd.px);
+      if (x0 < xb) { left = row + x0; lbytes = (xb - x0) * (int)sizeof(T); }
+      if (xc < xd) { right = row + sd.xl + (xc - sd.xr); rbytes = (xd - xc) * (int)sizeof(T); }
+    }
+    if (ctl & CTL_PF_YZ) {
+      wbytes = min(TX, sd.px - x0) * (int)sizeof(T);
+      if (y < sd.yl || y >= sd.yr) {
+        const int ys = y < sd.yl ? y : sd.yl + (y - sd.yr);
+        yrow = sd.psi_y + var * sd.psy + (long long)ys * sd.px + x0;
+      }
+      zrow = sd.psi_z + var * sd.psz + (long long)y * sd.px + x0;
+    }
+  }
+  __device__ __forceinline__ void plane(int k) const {
+    if (k < 0 || k >= nz) return;
+    if (lbytes) prefetch_l1(left + k * pstride, lbytes);
+    if (rbytes) prefetch_l1(right + k * pstride, rbytes);
+    if (yrow) prefetch_l2_bulk(yrow + k * ystride, wbytes);
+    if (zrow && (k < zl || k >= zr)) prefetch_l2_bulk(zrow + (k < zl ? k : zl + (k - zr)) * zstride, wbytes);
+  }
+};
+
+// Producer warp: walks the block's items and issues every plane's loads
+// (lane 0) and the plane's memory-variable prefetches (all lanes).  Load n
+// goes to stage n % NS; before reusing a stage lane 0 waits for the
+// consumers' release of load n - NS on that stage's empty barrier.  Item i
+// contributes planes k0 .. k1 (k1 is the look-ahead plane, possibly nz,
+// which the TMA fills with zeros).
+template <int NS, typename Issue, typename Prefetch>
 __device__ __forceinline__ void produce(const Item *__restrict__ items, int2 range, uint64_t *full, uint64_t *empty,
-                                        Issue issue, unsigned *__restrict__ err, int ctl) {
+                                        Issue issue, Prefetch &prefetch, unsigned *__restrict__ err, int ctl,
+                                        int lane) {
   if (ctl & CTL_WITHHOLD_LOADS) return;  // test mode: no stage is ever filled
   long long n = 0;
   bool ok = true;
   for (int ii = range.x; ii < range.y && ok; ++ii) {
     const Item it = items[ii];
+    prefetch.begin(it);
     for (int k = it.k0; k <= it.k1; ++k, ++n) {
       const int slot = (int)(n % NS);
-      if (n >= NS && !mbar_wait_bounded(&empty[slot], (uint32_t)(((n / NS) - 1) & 1))) {
+      int good = 1;
+      if (lane == 0 && n >= NS) good = mbar_wait_bounded(&empty[slot], (uint32_t)(((n / NS) - 1) & 1));
+      if (!__shfl_sync(0xffffffffu, good, 0)) {
         ok = false;
         break;
       }
-      issue(it, k, slot, &full[slot]);
+      if (lane == 0) issue(it, k, slot, &full[slot]);
+      prefetch.plane(k);
     }
   }
+  if (lane != 0) return;
   if (!ok) atomicOr(err, DEV_ERR_TIMEOUT);
   // the block must not exit with copies in flight
   for (long long q = (n > NS ? n - NS : 0); q < n; ++q)
@@ -121,12 +196,12 @@ __device__ __forceinline__ void produce(const Item *__restrict__ items, int2 ran
 // ----------------------------------------------------------- stress ----
 // (tick and dtick are unused by the stress half-step; the parameter list is
 // shared with the velocity kernel so both launch from one argument array)
-template <typename T, int TX, int TY, int NS>
-__global__ void __launch_bounds__(Geo<T, TX, TY, NS>::THREADS, Geo<T, TX, TY, NS>::MINB)
+template <typename T, int TX, int TY, int NS, int CPT, int MB>
+__global__ void __launch_bounds__(Geo<T, TX, TY, NS, CPT, MB>::THREADS, Geo<T, TX, TY, NS, CPT, MB>::MINB)
     stress_kernel(const ShotDesc<T> *__restrict__ shots, const ShotMaps *__restrict__ maps,
                   const Item *__restrict__ items, const int2 *__restrict__ ranges, int tick,
                   const int *__restrict__ dtick, unsigned *__restrict__ err, int ctl) {
-  using G = Geo<T, TX, TY, NS>;
+  using G = Geo<T, TX, TY, NS, CPT, MB>;
   constexpr int V = G::VEC, H = G::H, WW = G::WW;
   extern __shared__ __align__(1024) unsigned char smem[];
   uint64_t *full = reinterpret_cast<uint64_t *>(smem + NS * G::S_STAGE);
@@ -146,7 +221,7 @@ __global__ void __launch_bounds__(Geo<T, TX, TY, NS>::THREADS, Geo<T, TX, TY, NS
   __syncthreads();
 
   if (tid >= G::NT) {  // producer warp
-    if (tid == G::NT) {
+    {
       auto issue = [&](const Item &it, int k, int slot, uint64_t *bar) {
         const int txs = tiles_x_of(shots[it.shot], TX);
         const int x0 = (it.tile % txs) * TX, y0 = (it.tile / txs) * TY;
@@ -162,14 +237,25 @@ __global__ void __launch_bounds__(Geo<T, TX, TY, NS>::THREADS, Geo<T, TX, TY, NS
 #pragma unroll
         for (int c = 0; c < 6; ++c) tma_load_3d(st + G::S_SIG + c * G::SC, &m[6 + c], x0, y0, k, bar);
       };
-      produce<NS>(items, range, full, empty, issue, err, ctl);
+      struct {
+        PsiPrefetch<T, TX, TY> pf;
+        const ShotDesc<T> *shots;
+        int lane, ctl;
+        __device__ __forceinline__ void begin(const Item &it) {
+          const ShotDesc<T> &sd = shots[it.shot];
+          const int txs = tiles_x_of(sd, TX);
+          pf.begin(sd, (it.tile % txs) * TX, (it.tile / txs) * TY, PSI_S0, lane, ctl);
+        }
+        __device__ __forceinline__ void plane(int k) const { pf.plane(k); }
+      } prefetch{{}, shots, tid - G::NT, ctl};
+      produce<NS>(items, range, full, empty, issue, prefetch, err, ctl, tid - G::NT);
     }
     return;
   }
 
   const int lane = tid & 31;
   const int tx = tid % G::NTX, ty = tid / G::NTX;
-  const unsigned long long wait_ns = ctl ? kTestWaitLimitNs : kWaitLimitNs;
+  const unsigned long long wait_ns = (ctl & CTL_WITHHOLD_LOADS) ? kTestWaitLimitNs : kWaitLimitNs;
   long long n = 0;  // index of the load holding the current plane
 
   for (int ii = range.x; ii < range.y; ++ii) {
@@ -212,7 +298,8 @@ __global__ void __launch_bounds__(Geo<T, TX, TY, NS>::THREADS, Geo<T, TX, TY, NS
 #pragma unroll
       for (int e = 0; e < V; ++e) { ax[e] = axh[e] = T(0); bx[e] = bxh[e] = ikx[e] = ikxh[e] = T(1); }
     }
-    const bool in_y = live && (y < sd.yl || y >= sd.yr);
+    const bool row_y = y < sd.yl || y >= sd.yr;   // the row lies in the y slab
+    const bool in_y = live && row_y;
     const int ys = y < sd.yl ? y : sd.yl + (y - sd.yr);
     T ay = 0, by = 1, iky = 1, ayh = 0, byh = 1, ikyh = 1;
     if (in_y) {
@@ -226,7 +313,8 @@ __global__ void __launch_bounds__(Geo<T, TX, TY, NS>::THREADS, Geo<T, TX, TY, NS
 
     for (int k = item.k0; k < item.k1; ++k) {
       // memory variables and z profile first: their latency overlaps the wait
-      const bool in_z = live && (k < zl || k >= zr);
+      const bool plane_z = k < zl || k >= zr;       // the plane lies in the z slab
+      const bool in_z = live && plane_z;
       const int zs = k < zl ? k : zl + (k - zr);
       T az = 0, bz = 1, ikz = 1, azh = 0, bzh = 1, ikzh = 1;
       if (in_z) {
@@ -320,90 +408,115 @@ __global__ void __launch_bounds__(Geo<T, TX, TY, NS>::THREADS, Geo<T, TX, TY, NS
 
       const bool yN = (y >= 1) && (k >= 1);   // normal stresses: j >= 2, k >= 2 (1-based)
       const bool yXY = (y <= ny - 2);         // sigma_xy and sigma_yz: j <= NY-1
+      // The y- and z-direction C-PML terms are evaluated only for rows /
+      // planes inside the slabs (elsewhere a = 0 and 1/K = 1 and the terms
+      // are exact no-ops).  Memory variables are updated whether or not the
+      // cell's stress is: a cell outside the update ranges never uses them.
+      auto compute = [&](auto PY, auto PZ) {
+        constexpr bool pyo = decltype(PY)::value, pzo = decltype(PZ)::value;
 #pragma unroll
-      for (int e = 0; e < V; ++e) {
-        const int x = xg + e;
-        const T vx_xp = (e < V - 1) ? vx_c[e + 1] : vx_e;
-        const T vy_xm = (e > 0) ? vy_c[e - 1] : vy_w;
-        const T vz_xm = (e > 0) ? vz_c[e - 1] : vz_w;
-        const T cs_xm = (e > 0) ? cs_c[e - 1] : cs_w;
-        const T rho_xm = (e > 0) ? rho_c[e - 1] : rho_w;
+        for (int e = 0; e < V; ++e) {
+          const int x = xg + e;
+          const T vx_xp = (e < V - 1) ? vx_c[e + 1] : vx_e;
+          const T vy_xm = (e > 0) ? vy_c[e - 1] : vy_w;
+          const T vz_xm = (e > 0) ? vz_c[e - 1] : vz_w;
+          const T cs_xm = (e > 0) ? cs_c[e - 1] : cs_w;
+          const T rho_xm = (e > 0) ? rho_c[e - 1] : rho_w;
 
-        // normal stresses, simpelmodel.cpp:378-413
-        {
-          const bool m = yN && (x <= nx - 2);
-          const T vp = cp_c[e], vs = cs_c[e], rhos = rho_c[e];
-          const T lambda = rhos * (vp * vp - T(2) * vs * vs);
-          const T l2m = rhos * vp * vp;
-          const T DT_l2m = dt * l2m, DT_l = dt * lambda;
-          T dvx_dx = (vx_xp - vx_c[e]) * idx;
-          T dvy_dy = (vy_c[e] - vy_ym[e]) * idy;
-          T dvz_dz = (vz_c[e] - vz_zm[e]) * idz;
-          const T qx = bxh[e] * px0[e] + axh[e] * dvx_dx;
-          const T qy = by * py0[e] + ay * dvy_dy;
-          const T qz = bz * pz0[e] + az * dvz_dz;
-          dvx_dx = dvx_dx * ikxh[e] + qx;
-          dvy_dy = dvy_dy * iky + qy;
-          dvz_dz = dvz_dz * ikz + qz;
-          if (m) {
-            px0[e] = qx; py0[e] = qy; pz0[e] = qz;
-            sxx[e] = DT_l2m * dvx_dx + DT_l * (dvy_dy + dvz_dz) + sxx[e];
-            syy[e] = DT_l * (dvx_dx + dvz_dz) + DT_l2m * dvy_dy + syy[e];
-            szz[e] = DT_l * (dvx_dx + dvy_dy) + DT_l2m * dvz_dz + szz[e];
+          // normal stresses, simpelmodel.cpp:378-413
+          {
+            const bool m = yN && (x <= nx - 2);
+            const T vp = cp_c[e], vs = cs_c[e], rhos = rho_c[e];
+            const T lambda = rhos * (vp * vp - T(2) * vs * vs);
+            const T l2m = rhos * vp * vp;
+            const T DT_l2m = dt * l2m, DT_l = dt * lambda;
+            T dvx_dx = (vx_xp - vx_c[e]) * idx;
+            T dvy_dy = (vy_c[e] - vy_ym[e]) * idy;
+            T dvz_dz = (vz_c[e] - vz_zm[e]) * idz;
+            const T qx = bxh[e] * px0[e] + axh[e] * dvx_dx;
+            dvx_dx = dvx_dx * ikxh[e] + qx;
+            px0[e] = qx;
+            if constexpr (pyo) {
+              const T qy = by * py0[e] + ay * dvy_dy;
+              dvy_dy = dvy_dy * iky + qy;
+              py0[e] = qy;
+            }
+            if constexpr (pzo) {
+              const T qz = bz * pz0[e] + az * dvz_dz;
+              dvz_dz = dvz_dz * ikz + qz;
+              pz0[e] = qz;
+            }
+            if (m) {
+              sxx[e] = DT_l2m * dvx_dx + DT_l * (dvy_dy + dvz_dz) + sxx[e];
+              syy[e] = DT_l * (dvx_dx + dvz_dz) + DT_l2m * dvy_dy + syy[e];
+              szz[e] = DT_l * (dvx_dx + dvy_dy) + DT_l2m * dvz_dz + szz[e];
+            }
           }
-        }
-        // sigma_xy, :416-442
-        {
-          const bool m = yXY && (x >= 1) && (x <= nx - 1);
-          const T vs = (cs_xm + cs_yp[e]) / T(2);
-          const T rhos = (rho_xm + rho_yp[e]) / T(2);
-          const T DT_mu = dt * (rhos * vs * vs);
-          T dvy_dx = (vy_c[e] - vy_xm) * idx;
-          T dvx_dy = (vx_yp[e] - vx_c[e]) * idy;
-          const T qx = bx[e] * px1[e] + ax[e] * dvy_dx;
-          const T qy = byh * py1[e] + ayh * dvx_dy;
-          dvy_dx = dvy_dx * ikx[e] + qx;
-          dvx_dy = dvx_dy * ikyh + qy;
-          if (m) {
-            px1[e] = qx; py1[e] = qy;
-            sxy[e] = DT_mu * (dvy_dx + dvx_dy) + sxy[e];
+          // sigma_xy, :416-442
+          {
+            const bool m = yXY && (x >= 1) && (x <= nx - 1);
+            const T vs = (cs_xm + cs_yp[e]) / T(2);
+            const T rhos = (rho_xm + rho_yp[e]) / T(2);
+            const T DT_mu = dt * (rhos * vs * vs);
+            T dvy_dx = (vy_c[e] - vy_xm) * idx;
+            T dvx_dy = (vx_yp[e] - vx_c[e]) * idy;
+            const T qx = bx[e] * px1[e] + ax[e] * dvy_dx;
+            dvy_dx = dvy_dx * ikx[e] + qx;
+            px1[e] = qx;
+            if constexpr (pyo) {
+              const T qy = byh * py1[e] + ayh * dvx_dy;
+              dvx_dy = dvx_dy * ikyh + qy;
+              py1[e] = qy;
+            }
+            if (m) sxy[e] = DT_mu * (dvy_dx + dvx_dy) + sxy[e];
           }
-        }
-        // sigma_xz, :445-471 (z+1 of plane nz-1 is the zero plane)
-        {
-          const bool m = (x >= 1) && (x <= nx - 1);
-          const T vs = (cs_xm + cs_zp[e]) / T(2);
-          const T rhos = (rho_xm + rho_zp[e]) / T(2);
-          const T DT_mu = dt * (rhos * vs * vs);
-          T dvz_dx = (vz_c[e] - vz_xm) * idx;
-          T dvx_dz = (vx_zp[e] - vx_c[e]) * idz;
-          const T qx = bx[e] * px2[e] + ax[e] * dvz_dx;
-          const T qz = bzh * pz1[e] + azh * dvx_dz;
-          dvz_dx = dvz_dx * ikx[e] + qx;
-          dvx_dz = dvx_dz * ikzh + qz;
-          if (m) {
-            px2[e] = qx; pz1[e] = qz;
-            sxz[e] = DT_mu * (dvz_dx + dvx_dz) + sxz[e];
+          // sigma_xz, :445-471 (z+1 of plane nz-1 is the zero plane)
+          {
+            const bool m = (x >= 1) && (x <= nx - 1);
+            const T vs = (cs_xm + cs_zp[e]) / T(2);
+            const T rhos = (rho_xm + rho_zp[e]) / T(2);
+            const T DT_mu = dt * (rhos * vs * vs);
+            T dvz_dx = (vz_c[e] - vz_xm) * idx;
+            T dvx_dz = (vx_zp[e] - vx_c[e]) * idz;
+            const T qx = bx[e] * px2[e] + ax[e] * dvz_dx;
+            dvz_dx = dvz_dx * ikx[e] + qx;
+            px2[e] = qx;
+            if constexpr (pzo) {
+              const T qz = bzh * pz1[e] + azh * dvx_dz;
+              dvx_dz = dvx_dz * ikzh + qz;
+              pz1[e] = qz;
+            }
+            if (m) sxz[e] = DT_mu * (dvz_dx + dvx_dz) + sxz[e];
           }
-        }
-        // sigma_yz, :473-498
-        {
-          const bool m = yXY && (x <= nx - 1);
-          const T vs = (cs_yp[e] + cs_zp[e]) / T(2);
-          const T rhos = (rho_yp[e] + rho_zp[e]) / T(2);
-          const T DT_mu = dt * (rhos * vs * vs);
-          T dvz_dy = (vz_yp[e] - vz_c[e]) * idy;
-          T dvy_dz = (vy_zp[e] - vy_c[e]) * idz;
-          const T qy = byh * py2[e] + ayh * dvz_dy;
-          const T qz = bzh * pz2[e] + azh * dvy_dz;
-          dvz_dy = dvz_dy * ikyh + qy;
-          dvy_dz = dvy_dz * ikzh + qz;
-          if (m) {
-            py2[e] = qy; pz2[e] = qz;
-            syz[e] = DT_mu * (dvz_dy + dvy_dz) + syz[e];
+          // sigma_yz, :473-498
+          {
+            const bool m = yXY && (x <= nx - 1);
+            const T vs = (cs_yp[e] + cs_zp[e]) / T(2);
+            const T rhos = (rho_yp[e] + rho_zp[e]) / T(2);
+            const T DT_mu = dt * (rhos * vs * vs);
+            T dvz_dy = (vz_yp[e] - vz_c[e]) * idy;
+            T dvy_dz = (vy_zp[e] - vy_c[e]) * idz;
+            if constexpr (pyo) {
+              const T qy = byh * py2[e] + ayh * dvz_dy;
+              dvz_dy = dvz_dy * ikyh + qy;
+              py2[e] = qy;
+            }
+            if constexpr (pzo) {
+              const T qz = bzh * pz2[e] + azh * dvy_dz;
+              dvy_dz = dvy_dz * ikzh + qz;
+              pz2[e] = qz;
+            }
+            if (m) syz[e] = DT_mu * (dvz_dy + dvy_dz) + syz[e];
           }
+          vz_zm[e] = vz_c[e];
         }
-        vz_zm[e] = vz_c[e];
+      };
+      if (row_y) {
+        if (plane_z) compute(std::true_type{}, std::true_type{});
+        else compute(std::true_type{}, std::false_type{});
+      } else {
+        if (plane_z) compute(std::false_type{}, std::true_type{});
+        else compute(std::false_type{}, std::false_type{});
       }
 
       if (live) {
@@ -436,12 +549,12 @@ __global__ void __launch_bounds__(Geo<T, TX, TY, NS>::THREADS, Geo<T, TX, TY, NS
 }
 
 // --------------------------------------------------------- velocity ----
-template <typename T, int TX, int TY, int NS>
-__global__ void __launch_bounds__(Geo<T, TX, TY, NS>::THREADS, Geo<T, TX, TY, NS>::MINB)
+template <typename T, int TX, int TY, int NS, int CPT, int MB>
+__global__ void __launch_bounds__(Geo<T, TX, TY, NS, CPT, MB>::THREADS, Geo<T, TX, TY, NS, CPT, MB>::MINB)
     velocity_kernel(const ShotDesc<T> *__restrict__ shots, const ShotMaps *__restrict__ maps,
                     const Item *__restrict__ items, const int2 *__restrict__ ranges, int tick,
                     const int *__restrict__ dtick, unsigned *__restrict__ err, int ctl) {
-  using G = Geo<T, TX, TY, NS>;
+  using G = Geo<T, TX, TY, NS, CPT, MB>;
   constexpr int V = G::VEC, H = G::H, WW = G::WW;
   extern __shared__ __align__(1024) unsigned char smem[];
   uint64_t *full = reinterpret_cast<uint64_t *>(smem + NS * G::V_STAGE);
@@ -461,7 +574,7 @@ __global__ void __launch_bounds__(Geo<T, TX, TY, NS>::THREADS, Geo<T, TX, TY, NS
   __syncthreads();
 
   if (tid >= G::NT) {  // producer warp
-    if (tid == G::NT) {
+    {
       auto issue = [&](const Item &it, int k, int slot, uint64_t *bar) {
         const int txs = tiles_x_of(shots[it.shot], TX);
         const int x0 = (it.tile % txs) * TX, y0 = (it.tile / txs) * TY;
@@ -478,14 +591,25 @@ __global__ void __launch_bounds__(Geo<T, TX, TY, NS>::THREADS, Geo<T, TX, TY, NS
 #pragma unroll
         for (int c = 0; c < 3; ++c) tma_load_3d(st + G::V_V + c * G::SC, &m[7 + c], x0, y0, k, bar);
       };
-      produce<NS>(items, range, full, empty, issue, err, ctl);
+      struct {
+        PsiPrefetch<T, TX, TY> pf;
+        const ShotDesc<T> *shots;
+        int lane, ctl;
+        __device__ __forceinline__ void begin(const Item &it) {
+          const ShotDesc<T> &sd = shots[it.shot];
+          const int txs = tiles_x_of(sd, TX);
+          pf.begin(sd, (it.tile % txs) * TX, (it.tile / txs) * TY, PSI_V0, lane, ctl);
+        }
+        __device__ __forceinline__ void plane(int k) const { pf.plane(k); }
+      } prefetch{{}, shots, tid - G::NT, ctl};
+      produce<NS>(items, range, full, empty, issue, prefetch, err, ctl, tid - G::NT);
     }
     return;
   }
 
   const int lane = tid & 31;
   const int tx = tid % G::NTX, ty = tid / G::NTX;
-  const unsigned long long wait_ns = ctl ? kTestWaitLimitNs : kWaitLimitNs;
+  const unsigned long long wait_ns = (ctl & CTL_WITHHOLD_LOADS) ? kTestWaitLimitNs : kWaitLimitNs;
   constexpr int CS = G::SC / (int)sizeof(T);
   // step counter: an argument for direct launches, device memory plus an
   // offset inside a replayable CUDA graph
@@ -539,7 +663,8 @@ __global__ void __launch_bounds__(Geo<T, TX, TY, NS>::THREADS, Geo<T, TX, TY, NS
 #pragma unroll
       for (int e = 0; e < V; ++e) { ax[e] = axh[e] = T(0); bx[e] = bxh[e] = ikx[e] = ikxh[e] = T(1); }
     }
-    const bool in_y = live && (y < sd.yl || y >= sd.yr);
+    const bool row_y = y < sd.yl || y >= sd.yr;   // the row lies in the y slab
+    const bool in_y = live && row_y;
     const int ys = y < sd.yl ? y : sd.yl + (y - sd.yr);
     T ay = 0, by = 1, iky = 1, ayh = 0, byh = 1, ikyh = 1;
     if (in_y) {
@@ -553,7 +678,8 @@ __global__ void __launch_bounds__(Geo<T, TX, TY, NS>::THREADS, Geo<T, TX, TY, NS
     const int sc1 = (ty + 1) * TX + tx * V;   // syz box (origin x0, y0-1)
 
     for (int k = item.k0; k < item.k1; ++k) {
-      const bool in_z = live && (k < zl || k >= zr);
+      const bool plane_z = k < zl || k >= zr;       // the plane lies in the z slab
+      const bool in_z = live && plane_z;
       const int zs = k < zl ? k : zl + (k - zr);
       T az = 0, bz = 1, ikz = 1, azh = 0, bzh = 1, ikzh = 1;
       if (in_z) {
@@ -647,75 +773,99 @@ __global__ void __launch_bounds__(Geo<T, TX, TY, NS>::THREADS, Geo<T, TX, TY, NS
       const bool mvy_yz = (y <= ny - 2) && (k >= 1);
       const bool mvz_yz = (y >= 1) && (k <= nz - 2);
       T rbx[V], rby[V], rbz[V];   // averaged densities (reused by the source)
+      // y/z C-PML terms only inside the slabs; memory variables updated
+      // whether or not the cell's velocity is (as in the stress half-step)
+      auto compute = [&](auto PY, auto PZ) {
+        constexpr bool pyo = decltype(PY)::value, pzo = decltype(PZ)::value;
 #pragma unroll
-      for (int e = 0; e < V; ++e) {
-        const int x = xg + e;
-        const T sxx_xm = (e > 0) ? sxx_c[e - 1] : sxx_w;
-        const T rho_xm = (e > 0) ? rho_c[e - 1] : rho_w;
-        const T sxy_xp = (e < V - 1) ? sxy_c[e + 1] : sxy_e;
-        const T sxz_xp = (e < V - 1) ? sxz_c[e + 1] : sxz_e;
-        // vx, simpelmodel.cpp:502-530
-        {
-          const bool m = mvx_yz && (x >= 1) && (x <= nx - 1);
-          const T rhos = (rho_c[e] + rho_xm) / T(2);
-          rbx[e] = rhos;
-          const T DT_over_rho = div_fast(dt, rhos);
-          T d1 = (sxx_c[e] - sxx_xm) * idx;
-          T d2 = (sxy_c[e] - sxy_ym[e]) * idy;
-          T d3 = (sxz_c[e] - sxz_zm[e]) * idz;
-          const T qx = bx[e] * px0[e] + ax[e] * d1;
-          const T qy = by * py0[e] + ay * d2;
-          const T qz = bz * pz0[e] + az * d3;
-          d1 = d1 * ikx[e] + qx;
-          d2 = d2 * iky + qy;
-          d3 = d3 * ikz + qz;
-          if (m) {
-            px0[e] = qx; py0[e] = qy; pz0[e] = qz;
-            vx[e] = DT_over_rho * (d1 + d2 + d3) + vx[e];
+        for (int e = 0; e < V; ++e) {
+          const int x = xg + e;
+          const T sxx_xm = (e > 0) ? sxx_c[e - 1] : sxx_w;
+          const T rho_xm = (e > 0) ? rho_c[e - 1] : rho_w;
+          const T sxy_xp = (e < V - 1) ? sxy_c[e + 1] : sxy_e;
+          const T sxz_xp = (e < V - 1) ? sxz_c[e + 1] : sxz_e;
+          // vx, simpelmodel.cpp:502-530
+          {
+            const bool m = mvx_yz && (x >= 1) && (x <= nx - 1);
+            const T rhos = (rho_c[e] + rho_xm) / T(2);
+            rbx[e] = rhos;
+            const T DT_over_rho = div_fast(dt, rhos);
+            T d1 = (sxx_c[e] - sxx_xm) * idx;
+            T d2 = (sxy_c[e] - sxy_ym[e]) * idy;
+            T d3 = (sxz_c[e] - sxz_zm[e]) * idz;
+            const T qx = bx[e] * px0[e] + ax[e] * d1;
+            d1 = d1 * ikx[e] + qx;
+            px0[e] = qx;
+            if constexpr (pyo) {
+              const T qy = by * py0[e] + ay * d2;
+              d2 = d2 * iky + qy;
+              py0[e] = qy;
+            }
+            if constexpr (pzo) {
+              const T qz = bz * pz0[e] + az * d3;
+              d3 = d3 * ikz + qz;
+              pz0[e] = qz;
+            }
+            if (m) vx[e] = DT_over_rho * (d1 + d2 + d3) + vx[e];
           }
-        }
-        // vy, :532-559
-        {
-          const bool m = mvy_yz && (x <= nx - 2);
-          const T rhos = (rho_c[e] + rho_yp[e]) / T(2);
-          rby[e] = rhos;
-          const T DT_over_rho = div_fast(dt, rhos);
-          T d1 = (sxy_xp - sxy_c[e]) * idx;
-          T d2 = (syy_yp[e] - syy_c[e]) * idy;
-          T d3 = (syz_c[e] - syz_zm[e]) * idz;
-          const T qx = bxh[e] * px1[e] + axh[e] * d1;
-          const T qy = byh * py1[e] + ayh * d2;
-          const T qz = bz * pz1[e] + az * d3;
-          d1 = d1 * ikxh[e] + qx;
-          d2 = d2 * ikyh + qy;
-          d3 = d3 * ikz + qz;
-          if (m) {
-            px1[e] = qx; py1[e] = qy; pz1[e] = qz;
-            vy[e] = DT_over_rho * (d1 + d2 + d3) + vy[e];
+          // vy, :532-559
+          {
+            const bool m = mvy_yz && (x <= nx - 2);
+            const T rhos = (rho_c[e] + rho_yp[e]) / T(2);
+            rby[e] = rhos;
+            const T DT_over_rho = div_fast(dt, rhos);
+            T d1 = (sxy_xp - sxy_c[e]) * idx;
+            T d2 = (syy_yp[e] - syy_c[e]) * idy;
+            T d3 = (syz_c[e] - syz_zm[e]) * idz;
+            const T qx = bxh[e] * px1[e] + axh[e] * d1;
+            d1 = d1 * ikxh[e] + qx;
+            px1[e] = qx;
+            if constexpr (pyo) {
+              const T qy = byh * py1[e] + ayh * d2;
+              d2 = d2 * ikyh + qy;
+              py1[e] = qy;
+            }
+            if constexpr (pzo) {
+              const T qz = bz * pz1[e] + az * d3;
+              d3 = d3 * ikz + qz;
+              pz1[e] = qz;
+            }
+            if (m) vy[e] = DT_over_rho * (d1 + d2 + d3) + vy[e];
           }
-        }
-        // vz, :563-590
-        {
-          const bool m = mvz_yz && (x <= nx - 2);
-          const T rhos = (rho_c[e] + rho_zp[e]) / T(2);
-          rbz[e] = rhos;
-          const T DT_over_rho = div_fast(dt, rhos);
-          T d1 = (sxz_xp - sxz_c[e]) * idx;
-          T d2 = (syz_c[e] - syz_ym[e]) * idy;
-          T d3 = (szz_zp[e] - szz_c[e]) * idz;
-          const T qx = bxh[e] * px2[e] + axh[e] * d1;
-          const T qy = by * py2[e] + ay * d2;
-          const T qz = bzh * pz2[e] + azh * d3;
-          d1 = d1 * ikxh[e] + qx;
-          d2 = d2 * iky + qy;
-          d3 = d3 * ikzh + qz;
-          if (m) {
-            px2[e] = qx; py2[e] = qy; pz2[e] = qz;
-            vz[e] = DT_over_rho * (d1 + d2 + d3) + vz[e];
+          // vz, :563-590
+          {
+            const bool m = mvz_yz && (x <= nx - 2);
+            const T rhos = (rho_c[e] + rho_zp[e]) / T(2);
+            rbz[e] = rhos;
+            const T DT_over_rho = div_fast(dt, rhos);
+            T d1 = (sxz_xp - sxz_c[e]) * idx;
+            T d2 = (syz_c[e] - syz_ym[e]) * idy;
+            T d3 = (szz_zp[e] - szz_c[e]) * idz;
+            const T qx = bxh[e] * px2[e] + axh[e] * d1;
+            d1 = d1 * ikxh[e] + qx;
+            px2[e] = qx;
+            if constexpr (pyo) {
+              const T qy = by * py2[e] + ay * d2;
+              d2 = d2 * iky + qy;
+              py2[e] = qy;
+            }
+            if constexpr (pzo) {
+              const T qz = bzh * pz2[e] + azh * d3;
+              d3 = d3 * ikzh + qz;
+              pz2[e] = qz;
+            }
+            if (m) vz[e] = DT_over_rho * (d1 + d2 + d3) + vz[e];
           }
+          sxz_zm[e] = sxz_c[e];
+          syz_zm[e] = syz_c[e];
         }
-        sxz_zm[e] = sxz_c[e];
-        syz_zm[e] = syz_c[e];
+      };
+      if (row_y) {
+        if (plane_z) compute(std::true_type{}, std::true_type{});
+        else compute(std::true_type{}, std::false_type{});
+      } else {
+        if (plane_z) compute(std::false_type{}, std::true_type{});
+        else compute(std::false_type{}, std::false_type{});
       }
 
       if (live) {
