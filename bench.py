@@ -233,10 +233,10 @@ def run_ours(args, rank, world, local):
     tune_info = {"source": "built-in default"}
     if not args.no_autotune:
         best, ms_best, cand = E.autotune([(p, cp, cs, rho)], steps=10)
-        tune = {"variant": best.variant, "schedule": best.schedule, "chunk": best.chunk}
+        tune = best.as_dict()
         v = E.variants()[best.variant]
         tune_info = {"source": "ela3d_autotune", "candidates": cand, "tile": [v.tile_x, v.tile_y],
-                     "stages": v.stages, "schedule": best.schedule, "chunk": best.chunk}
+                     "stages": v.stages, "schedule": best.schedule, "chunk": best.chunk, "prefetch": best.prefetch}
     clocks = ClockSampler(local)
     plan = E.Plan(p, cp, cs, rho, **tune)
     plan.run(args.warmup)
@@ -327,7 +327,7 @@ def batched_shots(args, single_value: float) -> dict:
     if not args.no_autotune:
         # tuned on 8 of the shots (the per-cell speed is what differs)
         best, _, cand = E.autotune([(p, cp, cs, rho) for p in shots[:8]], steps=5)
-        tune = {"variant": best.variant, "schedule": best.schedule, "chunk": best.chunk}
+        tune = best.as_dict()
         tune_info = {"source": "ela3d_autotune on 8 of the shots", "candidates": cand, **tune}
     t0 = time.perf_counter()
     with E.Batch([(p, cp, cs, rho) for p in shots], **tune) as b:
@@ -367,7 +367,7 @@ def uneven_batch(args) -> dict:
     if not args.no_autotune:
         # tuned on every sixth instance (a cross-section of the sizes)
         best, _, cand = E.autotune(inst[::6], steps=5)
-        tune = {"variant": best.variant, "schedule": best.schedule, "chunk": best.chunk}
+        tune = best.as_dict()
         tune_info = {"source": "ela3d_autotune on every sixth instance", "candidates": cand, **tune}
     alone_s = 0.0
     for p, cp, cs, rho in inst:

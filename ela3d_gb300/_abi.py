@@ -85,8 +85,16 @@ class VariantInfo(ctypes.Structure):
 
 
 class Tuning(ctypes.Structure):
+    """ela3d_tuning; -1 / 0 fields leave the choice to the library."""
     _fields_ = [("variant", ctypes.c_int32), ("schedule", ctypes.c_int32), ("chunk", ctypes.c_int32),
-                ("blocks_per_sm", ctypes.c_int32)]
+                ("blocks_per_sm", ctypes.c_int32), ("prefetch", ctypes.c_int32)]
+
+    def __init__(self, variant: int = -1, schedule: int = -1, chunk: int = 0, blocks_per_sm: int = -1,
+                 prefetch: int = -1):
+        super().__init__(variant, schedule, chunk, blocks_per_sm, prefetch)
+
+    def as_dict(self) -> dict:
+        return {"variant": self.variant, "schedule": self.schedule, "chunk": self.chunk, "prefetch": self.prefetch}
 
 
 def variants() -> list[VariantInfo]:
@@ -196,7 +204,8 @@ class Plan:
     """One shot resident on the GPU (ela3d_plan_create / ela3d_run / ...)."""
 
     def __init__(self, params: ShotParams, cp: np.ndarray, cs: np.ndarray, rho: np.ndarray,
-                 variant: int = -1, schedule: int = -1, chunk: int = 0, blocks_per_sm: int = -1):
+                 variant: int = -1, schedule: int = -1, chunk: int = 0, blocks_per_sm: int = -1,
+                 prefetch: int = -1):
         lib = load_library()
         self._lib = lib
         self.params = params
@@ -206,14 +215,14 @@ class Plan:
             raise ValueError("model arrays must hold nx*ny*nz float32 values")
         c, rec = params.to_c()
         h = ctypes.c_void_p()
-        t = Tuning(variant, schedule, chunk, blocks_per_sm)
+        t = Tuning(variant, schedule, chunk, blocks_per_sm, prefetch)
         _check(lib.ela3d_plan_create_tuned(ctypes.byref(c), _ptr(models[0]), _ptr(models[1]), _ptr(models[2]),
                                            ctypes.byref(t), ctypes.byref(h)), "ela3d_plan_create")
         self._h = h
 
     @classmethod
     def from_model(cls, params: ShotParams, spec: dict, variant: int = -1, schedule: int = -1,
-                   chunk: int = 0) -> "Plan":
+                   chunk: int = 0, prefetch: int = -1) -> "Plan":
         """A plan whose model is generated on the device (ela3d_plan_create_model)."""
         self = cls.__new__(cls)
         lib = load_library()
@@ -221,7 +230,7 @@ class Plan:
         self.params = params
         c, rec = params.to_c()
         m = ModelSpec.from_dict(spec)
-        t = Tuning(variant, schedule, chunk, -1)
+        t = Tuning(variant, schedule, chunk, -1, prefetch)
         h = ctypes.c_void_p()
         _check(lib.ela3d_plan_create_model(ctypes.byref(c), ctypes.byref(m), ctypes.byref(t), ctypes.byref(h)),
                "ela3d_plan_create_model")
@@ -315,7 +324,8 @@ class Batch:
     (ShotParams, cp, cs, rho); passing the same model arrays for several
     shots stores that model once on the device."""
 
-    def __init__(self, shots, variant: int = -1, schedule: int = -1, chunk: int = 0, blocks_per_sm: int = -1):
+    def __init__(self, shots, variant: int = -1, schedule: int = -1, chunk: int = 0, blocks_per_sm: int = -1,
+                 prefetch: int = -1):
         lib = load_library()
         self._lib = lib
         self.params = [s[0] for s in shots]
@@ -337,7 +347,7 @@ class Batch:
                     seen[id(arr)] = m
                     keep.append(m)
                 ptrs[key][i] = m.ctypes.data
-        t = Tuning(variant, schedule, chunk, blocks_per_sm)
+        t = Tuning(variant, schedule, chunk, blocks_per_sm, prefetch)
         h = ctypes.c_void_p()
         _check(lib.ela3d_batch_create(n, structs, ptrs["cp"], ptrs["cs"], ptrs["rho"], ctypes.byref(t),
                                       ctypes.byref(h)), "ela3d_batch_create")
@@ -412,7 +422,7 @@ class Server:
     """Continuous-batching request loop (ela3d_server_*)."""
 
     def __init__(self, hbm_budget_bytes: int = 0, max_active: int = 0, steps_per_round: int = 50,
-                 precision: int = 0, variant: int = -1, schedule: int = -1, chunk: int = 0):
+                 precision: int = 0, variant: int = -1, schedule: int = -1, chunk: int = 0, prefetch: int = -1):
         lib = load_library()
         self._lib = lib
         cfg = ServerConfig()
@@ -421,7 +431,7 @@ class Server:
         cfg.max_active = max_active
         cfg.steps_per_round = steps_per_round
         cfg.precision = precision
-        cfg.tune = Tuning(variant, schedule, chunk, -1)
+        cfg.tune = Tuning(variant, schedule, chunk, -1, prefetch)
         h = ctypes.c_void_p()
         _check(lib.ela3d_server_create(ctypes.byref(cfg), ctypes.byref(h)), "ela3d_server_create")
         self._h = h

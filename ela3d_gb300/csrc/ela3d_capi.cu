@@ -124,6 +124,7 @@ static TuneChoice resolve_tuning(const std::vector<ela3d_params> &ps, const floa
   if (t->schedule >= 0) c.kind = t->schedule;
   if (t->chunk > 0) c.chunk = t->chunk;
   if (t->blocks_per_sm >= 0) c.blocks_per_sm = t->blocks_per_sm;
+  if (t->prefetch >= 0) c.prefetch = t->prefetch & (CTL_PF_X | CTL_PF_YZ);
   return c;
 }
 

@@ -138,10 +138,10 @@ TuneChoice default_choice(int fp64, int nx, int ny, int nz) {
   int n = 0;
   const Variant *v = variants(&n);
   // first variant of the precision (the list is ordered best first for
-  // large grids), z-chunks of 16 planes dealt round-robin
+  // large grids), z-chunks of 10 planes dealt round-robin, both prefetches
   for (int i = 0; i < n; ++i)
-    if ((v[i].fp64 != 0) == (fp64 != 0)) return {i, 1, 16, 0};
-  return {0, 1, 16, 0};
+    if ((v[i].fp64 != 0) == (fp64 != 0)) return {i, 1, 10, 0, kPrefetchDefault};
+  return {0, 1, 10, 0, kPrefetchDefault};
 }
 
 // ------------------------------------------------------------ TMA maps --
@@ -251,7 +251,8 @@ class Engine final : public EngineBase {
     CK(cudaMalloc(&d_energy_, sizeof(double)));
     CK(cudaMalloc(&d_tick_, sizeof(int)));
     CK(cudaMemset(d_tick_, 0, sizeof(int)));
-    if (const char *e = std::getenv("ELA3D_PSI_PREFETCH")) prefetch_ = std::atoi(e) & (CTL_PF_X | CTL_PF_YZ);
+    // ELA3D_PSI_PREFETCH=<bits> overrides the tuned prefetch mode (experiments)
+    if (const char *e = std::getenv("ELA3D_PSI_PREFETCH")) prefetch_env_ = std::atoi(e) & (CTL_PF_X | CTL_PF_YZ);
     return ELA3D_OK;
   }
 
@@ -551,6 +552,7 @@ class Engine final : public EngineBase {
     if (c.variant < 0 || c.variant >= nv || vs[c.variant].fp64 != (sizeof(T) == 8)) BAD("bad kernel variant");
     var_ = &vs[c.variant];
     choice_ = c;
+    prefetch_ = prefetch_env_ >= 0 ? prefetch_env_ : (c.prefetch & (CTL_PF_X | CTL_PF_YZ));
     for (auto &sp : shots_) {
       ela3d_status st = encode_shot_maps(*sp);
       if (st != ELA3D_OK) return st;
@@ -567,6 +569,23 @@ class Engine final : public EngineBase {
       if (st != ELA3D_OK) return st;
     }
     finalized_ = true;
+    return rebuild_schedule();
+  }
+
+  ela3d_status retune(const TuneChoice &c) override {
+    if (!finalized_) return finalize(&c);
+    int nv = 0;
+    const Variant *vs = variants(&nv);
+    if (c.variant < 0 || c.variant >= nv || var_ != &vs[c.variant]) BAD("retune keeps the kernel variant");
+    choice_ = c;
+    prefetch_ = prefetch_env_ >= 0 ? prefetch_env_ : (c.prefetch & (CTL_PF_X | CTL_PF_YZ));
+    int occ_s = 0, occ_v = 0;
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_s, var_->stress, var_->threads, var_->stress_smem));
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_v, var_->velocity, var_->threads, var_->vel_smem));
+    per_sm_ = std::max(1, std::min(occ_s, occ_v));
+    if (c.blocks_per_sm > 0) per_sm_ = std::min(per_sm_, c.blocks_per_sm);
+    sched_valid_ = false;
+    sched_key_.clear();
     return rebuild_schedule();
   }
 
@@ -982,7 +1001,8 @@ class Engine final : public EngineBase {
   bool sched_valid_ = false, retire_ = false;
   int tick_ = 0;
   int inject_ = 0;   // steps left whose launches withhold their loads (test hook)
-  int prefetch_ = CTL_PF_X | CTL_PF_YZ;  // memory-variable prefetch hints (x slab to L1, y/z slabs to L2)
+  int prefetch_ = kPrefetchDefault;  // memory-variable prefetch hints (x slab to L1, y/z slabs to L2)
+  int prefetch_env_ = -1;
   int *d_tick_ = nullptr;
   cudaGraphExec_t gexec_ = nullptr;
   bool use_graphs_ = true, capturing_ = false;

@@ -42,13 +42,15 @@ struct ShotShape {
 void build_schedule(const std::vector<ShotShape> &shots, int tx, int ty, int kind, int chunk,
                     int max_blocks, std::vector<Item> *items, std::vector<int2> *ranges);
 
-// Chooses the kernel variant for a grid: the measured autotuner table when
-// one was loaded, else a fixed default per precision.
+// A kernel variant, its work schedule and the memory-variable prefetch mode.
+constexpr int kPrefetchDefault = CTL_PF_X | CTL_PF_YZ;
 struct TuneChoice {
   int variant;     // index into variants()
   int kind, chunk; // schedule
   int blocks_per_sm;  // 0 = occupancy limit
+  int prefetch = kPrefetchDefault;  // CTL_PF_* bits
 };
+// Built-in choice when the autotuner's cache has none for the workload.
 TuneChoice default_choice(int fp64, int nx, int ny, int nz);
 
 // Autotuner (ela3d_tune.cu): process-wide cache of measured best choices
@@ -67,6 +69,9 @@ class EngineBase {
   virtual ela3d_status add_shot(const ela3d_params &p, const float *cp, const float *cs, const float *rho,
                                 int shared_model_of, const ModelSpec *spec = nullptr) = 0;
   virtual ela3d_status finalize(const TuneChoice *choice) = 0;
+  // A finalized engine switches to another schedule / prefetch mode of the
+  // same kernel variant (the autotuner's inner loop).
+  virtual ela3d_status retune(const TuneChoice &choice) = 0;
   virtual ela3d_status enqueue(int nsteps) = 0;
   // enqueue bracketed by events on the engine's stream; waits, returns ms
   virtual ela3d_status run_timed(int nsteps, double *ms) = 0;

@@ -33,10 +33,14 @@ void load_locked() {
   if (!f) return;
   FILE *fp = std::fopen(f, "r");
   if (!fp) return;
-  char key[512];
-  TuneChoice c{};
-  while (std::fscanf(fp, "%511s %d %d %d %d", key, &c.variant, &c.kind, &c.chunk, &c.blocks_per_sm) == 5)
-    g_cache[key] = c;
+  // one line per workload: key variant kind chunk blocks_per_sm prefetch
+  char line[1024], key[512];
+  while (std::fgets(line, sizeof line, fp)) {
+    TuneChoice c{};
+    if (std::sscanf(line, "%511s %d %d %d %d %d", key, &c.variant, &c.kind, &c.chunk, &c.blocks_per_sm,
+                    &c.prefetch) == 6)
+      g_cache[key] = c;
+  }
   std::fclose(fp);
 }
 
@@ -46,8 +50,8 @@ void save_locked() {
   FILE *fp = std::fopen(f, "w");
   if (!fp) return;
   for (auto &kv : g_cache)
-    std::fprintf(fp, "%s %d %d %d %d\n", kv.first.c_str(), kv.second.variant, kv.second.kind, kv.second.chunk,
-                 kv.second.blocks_per_sm);
+    std::fprintf(fp, "%s %d %d %d %d %d\n", kv.first.c_str(), kv.second.variant, kv.second.kind,
+                 kv.second.chunk, kv.second.blocks_per_sm, kv.second.prefetch);
   std::fclose(fp);
 }
 }  // namespace
@@ -90,13 +94,17 @@ void tune_store(const std::vector<ela3d_params> &ps, const TuneChoice &c) {
   save_locked();
 }
 
-// Candidate schedules for a workload.
+// Candidate schedules and prefetch modes for a workload: contiguous shares;
+// z-chunks of 6..32 planes round-robin; for batches also shot-interleaved
+// chunks; each with both memory-variable prefetches or the x slab's only.
 static std::vector<TuneChoice> schedules(int nshots) {
   std::vector<TuneChoice> v;
-  v.push_back({0, 0, 16, 0});
-  for (int ch : {8, 16, 32}) v.push_back({0, 1, ch, 0});
-  if (nshots > 1)
-    for (int ch : {8, 16}) v.push_back({0, 2, ch, 0});
+  for (int pf : {kPrefetchDefault, (int)CTL_PF_X}) {
+    v.push_back({0, 0, 16, 0, pf});
+    for (int ch : {6, 8, 10, 12, 16, 32}) v.push_back({0, 1, ch, 0, pf});
+    if (nshots > 1)
+      for (int ch : {8, 16}) v.push_back({0, 2, ch, 0, pf});
+  }
   return v;
 }
 
@@ -111,25 +119,29 @@ ela3d_status autotune(const std::vector<ela3d_params> &ps, const std::vector<con
   TuneChoice bc{-1, 0, 0, 0};
   for (int v = 0; v < nv; ++v) {
     if (vs[v].fp64 != fp64) continue;
+    // one engine per variant (the tensor maps depend on the tile); the
+    // schedules and prefetch modes are switched in place
+    ela3d_status st;
+    auto eng = make_engine(fp64, &st);
+    for (size_t q = 0; q < ps.size() && st == ELA3D_OK; ++q) {
+      int share = -1;
+      for (size_t j = 0; j < q && share < 0; ++j)
+        if (cp[j] == cp[q] && cs[j] == cs[q] && rho[j] == rho[q] && ps[j].nx == ps[q].nx &&
+            ps[j].ny == ps[q].ny && ps[j].nz == ps[q].nz)
+          share = (int)j;
+      st = eng->add_shot(ps[q], cp[q], cs[q], rho[q], share);
+    }
+    if (st == ELA3D_ERR_OOM) return st;
+    if (st != ELA3D_OK) continue;
     for (TuneChoice c : schedules((int)ps.size())) {
       c.variant = v;
-      ela3d_status st;
-      auto eng = make_engine(fp64, &st);
-      for (size_t q = 0; q < ps.size() && st == ELA3D_OK; ++q) {
-        int share = -1;
-        for (size_t j = 0; j < q && share < 0; ++j)
-          if (cp[j] == cp[q] && cs[j] == cs[q] && rho[j] == rho[q] && ps[j].nx == ps[q].nx &&
-              ps[j].ny == ps[q].ny && ps[j].nz == ps[q].nz)
-            share = (int)j;
-        st = eng->add_shot(ps[q], cp[q], cs[q], rho[q], share);
-      }
-      if (st == ELA3D_OK) st = eng->finalize(&c);
+      st = eng->retune(c);
       if (st == ELA3D_OK) st = eng->enqueue(2);  // warm-up
       if (st == ELA3D_OK) st = eng->sync();
       double ms = 0.0;
       if (st == ELA3D_OK) st = eng->run_timed(steps, &ms);
       if (st == ELA3D_ERR_OOM) return st;
-      if (st != ELA3D_OK) continue;  // a candidate that does not run is skipped
+      if (st != ELA3D_OK) break;  // a variant that does not run is skipped
       if (table) table->push_back({c, ms});
       if (ms < best_t) {
         best_t = ms;
@@ -170,6 +182,7 @@ extern "C" ela3d_status ela3d_autotune(int32_t nshots, const ela3d_params *param
   best->schedule = bc.kind;
   best->chunk = bc.chunk;
   best->blocks_per_sm = bc.blocks_per_sm;
+  best->prefetch = bc.prefetch;
   if (candidates) *candidates = (int32_t)table.size();
   return ELA3D_OK;
 }

@@ -184,9 +184,12 @@ typedef struct ela3d_variant_info {
  * fields select the built-in default. */
 typedef struct ela3d_tuning {
     int32_t variant;        /* index < ela3d_variant_count(), or -1 */
-    int32_t schedule;       /* 0, 1, or -1 */
-    int32_t chunk;          /* planes per z-chunk for schedule 1 */
+    int32_t schedule;       /* 0, 1, 2, or -1 */
+    int32_t chunk;          /* planes per z-chunk for schedules 1 and 2 */
     int32_t blocks_per_sm;  /* cap on resident blocks per SM, 0 = occupancy limit */
+    int32_t prefetch;       /* prefetch of the C-PML memory variables by the
+                               loading warp: bit 1 (2) x slab into L1, bit 2 (4)
+                               y and z slabs into L2; -1 = default (6) */
 } ela3d_tuning;
 
 /* Times every compiled variant with the candidate schedules on these shots

@@ -92,13 +92,13 @@ def test_variants_and_schedules_bit_identical(built):
     for i, v in enumerate(ela3d_gb300.variants()):
         if v.fp64:
             continue
-        for sched, chunk in ((0, 0), (1, 5), (1, 64)):
-            seis, fields = run_gpu(p, cp, cs, rho, variant=i, schedule=sched, chunk=chunk)
+        for sched, chunk, pf in ((0, 0, 6), (1, 5, 0), (1, 64, 2), (1, 7, 4)):
+            seis, fields = run_gpu(p, cp, cs, rho, variant=i, schedule=sched, chunk=chunk, prefetch=pf)
             if ref is None:
                 ref = (seis, fields)
             else:
-                assert np.array_equal(seis, ref[0]), (i, sched, chunk)
-                assert np.array_equal(fields, ref[1]), (i, sched, chunk)
+                assert np.array_equal(seis, ref[0]), (i, sched, chunk, pf)
+                assert np.array_equal(fields, ref[1]), (i, sched, chunk, pf)
 
 
 def test_resume_equals_single_run(built):

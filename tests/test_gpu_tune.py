@@ -14,10 +14,11 @@ def test_autotune_picks_a_valid_choice_and_results_do_not_change(built, tmp_path
     p, cp, cs, rho = configs.anticline_256(nstep=60, n=96)
     best, ms, cand = E.autotune([(p, cp, cs, rho)], steps=5)
     n32 = sum(1 for v in E.variants() if not v.fp64)
-    assert cand == n32 * 4          # four schedules for a single shot
+    assert cand == n32 * 14         # seven schedules x two prefetch modes for a single shot
     assert 0 <= best.variant < len(E.variants()) and not E.variants()[best.variant].fp64
     assert ms > 0
-    with E.Plan(p, cp, cs, rho, variant=best.variant, schedule=best.schedule, chunk=best.chunk) as a:
+    assert best.prefetch in (2, 6)
+    with E.Plan(p, cp, cs, rho, **best.as_dict()) as a:
         a.run(60)
         sa = a.seismograms()
     with E.Plan(p, cp, cs, rho) as b:   # picks the cached choice
@@ -33,5 +34,5 @@ def test_autotune_batch_includes_interleaved_schedules(built):
     shots, cp, cs, rho = configs.anticline_256_shots(4, nstep=20, n=64)
     best, ms, cand = E.autotune([(s, cp, cs, rho) for s in shots], steps=3)
     n32 = sum(1 for v in E.variants() if not v.fp64)
-    assert cand == n32 * 6
+    assert cand == n32 * 18         # nine schedules x two prefetch modes for a batch
     assert best.schedule in (0, 1, 2)
