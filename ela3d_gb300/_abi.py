@@ -31,6 +31,8 @@ SIGNATURES = [
     ("ela3d_get_seismograms", _c.c_int, [_P, _P]),
     ("ela3d_get_seismograms_f64", _c.c_int, [_P, _P]),
     ("ela3d_get_field", _c.c_int, [_P, _c.c_int32, _P]),
+    ("ela3d_get_source_trace", _c.c_int, [_P, _P]),
+    ("ela3d_get_source_trace_f64", _c.c_int, [_P, _P]),
     ("ela3d_get_field_f64", _c.c_int, [_P, _c.c_int32, _P]),
     ("ela3d_energy", _c.c_int, [_P, _c.POINTER(_c.c_double)]),
     ("ela3d_plan_info_get", _c.c_int, [_P, _P]),
@@ -48,6 +50,7 @@ SIGNATURES = [
     ("ela3d_batch_run_timed", _c.c_int, [_P, _c.c_int32, _c.POINTER(_c.c_double)]),
     ("ela3d_batch_get_seismograms", _c.c_int, [_P, _c.c_int32, _P]),
     ("ela3d_batch_get_field", _c.c_int, [_P, _c.c_int32, _c.c_int32, _P]),
+    ("ela3d_batch_get_source_trace", _c.c_int, [_P, _c.c_int32, _P]),
     ("ela3d_batch_info", _c.c_int, [_P, _c.c_int32, _P]),
     ("ela3d_batch_destroy", _c.c_int, [_P]),
     ("ela3d_server_config_default", _c.c_int, [_P]),
@@ -265,6 +268,14 @@ class Plan:
             _check(fn(self._h, _ptr(out)), "ela3d_get_seismograms")
         return out
 
+    def source_trace(self, fp64: bool = False) -> np.ndarray:
+        """[3, nstep + 1]: the source cell's injected components after each
+        step's injection (sxx syy szz explosive, vx vy vz force)."""
+        out = np.zeros((3, self.params.nstep + 1), np.float64 if fp64 else np.float32)
+        fn = self._lib.ela3d_get_source_trace_f64 if fp64 else self._lib.ela3d_get_source_trace
+        _check(fn(self._h, _ptr(out)), "ela3d_get_source_trace")
+        return out
+
     def field(self, comp: int, fp64: bool = False) -> np.ndarray:
         p = self.params
         out = np.empty((p.nz, p.ny, p.nx), np.float64 if fp64 else np.float32)
@@ -366,6 +377,11 @@ class Batch:
         out = np.zeros((p.nrec, 3, p.nsamp), np.float32)
         if out.size:
             _check(self._lib.ela3d_batch_get_seismograms(self._h, shot, _ptr(out)), "ela3d_batch_get_seismograms")
+        return out
+
+    def source_trace(self, shot: int) -> np.ndarray:
+        out = np.zeros((3, self.params[shot].nstep + 1), np.float32)
+        _check(self._lib.ela3d_batch_get_source_trace(self._h, shot, _ptr(out)), "ela3d_batch_get_source_trace")
         return out
 
     def field(self, shot: int, comp: int) -> np.ndarray:

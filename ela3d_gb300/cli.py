@@ -16,7 +16,9 @@ receivers written to seis.npy as [nrec, 3, nsamp]).
 
 Outputs (in --outdir): rechorvx.txt rechorvy.txt rechorvz.txt when ngatx
 and ngaty are given (:625-671), vz%05i.bin vy%05i.bin vx%05i.bin every
-it_output steps (:673-725), seis.npy for the rec lines.
+it_output steps (:673-725), recsrcx.txt recsrcy.txt recsrcz.txt (the
+source-point trace of elatic_3d_unified_cuda_memory.cu:1202-1223), seis.npy
+for the rec lines.
 """
 from __future__ import annotations
 
@@ -89,7 +91,8 @@ def run(params_path: str, outdir: str, fp64: bool = False) -> dict:
                 fields = [plan.field(c, fp64=fp64) for c in range(3)]
                 refio.write_snapshots(outdir, done, fields[0], fields[1], fields[2], dtype=dt)
         seis = plan.seismograms()
-    written = {}
+        trace = plan.source_trace(fp64=fp64)
+    written = {"recsrc": refio.write_recsrc(outdir, trace)}
     if slots is not None:
         written["rechor"] = refio.write_rechor(outdir, seis[: len(cells)], slots)
     if user_rec.size:

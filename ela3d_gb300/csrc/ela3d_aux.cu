@@ -107,9 +107,17 @@ __global__ void explosive_kernel(const ShotDesc<T> *shots, int nshots, int tick,
   const T l2m = sd.rho[o] * sd.cp[o] * sd.cp[o];
   const T s = sd.stf[it - 1];
   const T fx = sd.expl_w[0] * s, fy = sd.expl_w[1] * s, fz = sd.expl_w[2] * s;
-  sd.f[3][o] = sd.f[3][o] + fx * sd.dt * l2m;
-  sd.f[4][o] = sd.f[4][o] + fy * sd.dt * l2m;
-  sd.f[5][o] = sd.f[5][o] + fz * sd.dt * l2m;
+  const T sxx = sd.f[3][o] + fx * sd.dt * l2m;
+  const T syy = sd.f[4][o] + fy * sd.dt * l2m;
+  const T szz = sd.f[5][o] + fz * sd.dt * l2m;
+  sd.f[3][o] = sxx;
+  sd.f[4][o] = syy;
+  sd.f[5][o] = szz;
+  // source-point trace (elatic_3d_unified_cuda_memory.cu:463-465)
+  const int ns = sd.nstep + 1;
+  sd.src_trace[it] = sxx;
+  sd.src_trace[ns + it] = syy;
+  sd.src_trace[2 * ns + it] = szz;
 }
 
 // Kinetic 1/2 rho |v|^2 plus isotropic strain energy

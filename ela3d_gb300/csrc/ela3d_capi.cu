@@ -267,6 +267,16 @@ ela3d_status ela3d_get_seismograms_f64(ela3d_plan *plan, double *out) {
   return plan->eng->seismograms(0, out, 1);
 }
 
+ela3d_status ela3d_get_source_trace(ela3d_plan *plan, float *out) {
+  if (!plan || !out) return ELA3D_ERR_INVALID_ARG;
+  return plan->eng->source_trace(0, out, 0);
+}
+
+ela3d_status ela3d_get_source_trace_f64(ela3d_plan *plan, double *out) {
+  if (!plan || !out) return ELA3D_ERR_INVALID_ARG;
+  return plan->eng->source_trace(0, out, 1);
+}
+
 ela3d_status ela3d_get_field(ela3d_plan *plan, int32_t comp, float *out) {
   if (!plan || !out) return ELA3D_ERR_INVALID_ARG;
   return plan->eng->field(0, comp, out, 0);
@@ -404,6 +414,11 @@ ela3d_status ela3d_batch_run_timed(ela3d_batch *b, int32_t nsteps, double *ms) {
 ela3d_status ela3d_batch_get_seismograms(ela3d_batch *b, int32_t shot, float *out) {
   if (!b || !out) return ELA3D_ERR_INVALID_ARG;
   return b->eng->seismograms(shot, out, 0);
+}
+
+ela3d_status ela3d_batch_get_source_trace(ela3d_batch *b, int32_t shot, float *out) {
+  if (!b || !out) return ELA3D_ERR_INVALID_ARG;
+  return b->eng->source_trace(shot, out, 0);
 }
 
 ela3d_status ela3d_batch_get_field(ela3d_batch *b, int32_t shot, int32_t comp, float *out) {

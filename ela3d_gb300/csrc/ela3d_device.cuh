@@ -74,6 +74,9 @@ struct ShotDesc {
   const int *rec_plane;      // nz+1 offsets into rec_sorted
   const int4 *rec_sorted;    // (i, j, k, receiver index) sorted by (k, j, i)
   T *seis;                   // [nrec][3][nsamp]
+  T *src_trace;              // [3][nstep + 1]: the source cell's injected components
+                             // (sxx syy szz, or vx vy vz for a force) after step it's
+                             // injection at index it; index 0 stays 0
 };
 
 // Tensor maps of one shot.  Box shapes (TX, TY = tile; H = 16 bytes of T):

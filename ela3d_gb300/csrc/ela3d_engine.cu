@@ -355,6 +355,7 @@ class Engine final : public EngineBase {
     const size_t o_rp = take((size_t)(nz + 1) * sizeof(int));
     const size_t o_rs = take(std::max<size_t>(1, nrec) * sizeof(int4));
     const size_t o_seis = take(std::max<size_t>(1, nrec * 3 * s.nsamp) * sizeof(T));
+    const size_t o_trace = take(3 * (size_t)(p.nstep + 1) * sizeof(T));
     s.pool_bytes = o;
     CK(cudaMalloc(&s.pool, s.pool_bytes));
     CK(cudaMemsetAsync(s.pool, 0, s.pool_bytes, stream_));
@@ -397,6 +398,7 @@ class Engine final : public EngineBase {
     d.rec_plane = reinterpret_cast<int *>(s.pool + o_rp);
     d.rec_sorted = reinterpret_cast<int4 *>(s.pool + o_rs);
     d.seis = reinterpret_cast<T *>(s.pool + o_seis);
+    d.src_trace = reinterpret_cast<T *>(s.pool + o_trace);
 
     // 3. model: generated on the device, or uploaded into the padded layout
     if (shared_model_of < 0 && spec) {
@@ -506,7 +508,8 @@ class Engine final : public EngineBase {
     const int64_t xw = std::min<int64_t>(px, w + 2 * V), yw = std::min<int64_t>(p.ny, w), zw = std::min<int64_t>(p.nz, w);
     int64_t b = 12 * cells + 6 * ((int64_t)p.nz * p.ny * xw + (int64_t)p.nz * yw * px + zw * (int64_t)p.ny * px);
     b = b * (int64_t)sizeof(T) + (int64_t)p.nrec * 3 * (p.nstep / std::max(1, p.sampgat)) * (int64_t)sizeof(T) +
-        (int64_t)p.nstep * (int64_t)sizeof(T) + 6 * (px + p.ny + p.nz) * (int64_t)sizeof(T) + 32 * 256;
+        (int64_t)p.nstep * (int64_t)sizeof(T) + 3 * (int64_t)(p.nstep + 1) * (int64_t)sizeof(T) +
+        6 * (px + p.ny + p.nz) * (int64_t)sizeof(T) + 32 * 256;
     return b;
   }
 
@@ -824,6 +827,17 @@ class Engine final : public EngineBase {
     if (n == 0) return ELA3D_OK;
     std::vector<T> h(n);
     CK(cudaMemcpyAsync(h.data(), s.d.seis, n * sizeof(T), cudaMemcpyDeviceToHost, stream_));
+    CK(cudaStreamSynchronize(stream_));
+    convert_out(h.data(), n, out, out_fp64);
+    return ELA3D_OK;
+  }
+
+  ela3d_status source_trace(int shot, void *out, int out_fp64) override {
+    if (shot < 0 || shot >= nshots() || !out) BAD("bad shot or output");
+    const Shot<T> &s = *shots_[shot];
+    const size_t n = 3 * (size_t)(s.p.nstep + 1);
+    std::vector<T> h(n);
+    CK(cudaMemcpyAsync(h.data(), s.d.src_trace, n * sizeof(T), cudaMemcpyDeviceToHost, stream_));
     CK(cudaStreamSynchronize(stream_));
     convert_out(h.data(), n, out, out_fp64);
     return ELA3D_OK;

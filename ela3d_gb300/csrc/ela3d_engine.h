@@ -78,6 +78,7 @@ class EngineBase {
   virtual ela3d_status sync() = 0;
   virtual ela3d_status seismograms(int shot, void *out, int out_fp64) = 0;
   virtual ela3d_status field(int shot, int comp, void *out, int out_fp64) = 0;
+  virtual ela3d_status source_trace(int shot, void *out, int out_fp64) = 0;
   virtual ela3d_status energy(int shot, double *out) = 0;
   virtual ela3d_status info(int shot, ela3d_plan_info *out) = 0;
   virtual ela3d_status set_timing(bool on) = 0;

@@ -903,13 +903,22 @@ __global__ void __launch_bounds__(Geo<T, TX, TY, NS, CPT, MB>::THREADS, Geo<T, T
           const int se = sd.src_i - xg;
           const bool wx = sd.src_w[0] != T(0), wy = sd.src_w[1] != T(0), wz = sd.src_w[2] != T(0);
           const T fx = sd.src_w[0] * s, fy = sd.src_w[1] * s, fz = sd.src_w[2] * s;
+          T tvx = vx[0], tvy = vy[0], tvz = vz[0];
 #pragma unroll
           for (int c = 0; c < V; ++c) {
             const bool hit = (c == se);
             vx[c] = (hit && wx) ? vx[c] + fx * dt / rbx[c] : vx[c];
             vy[c] = (hit && wy) ? vy[c] + fy * dt / rby[c] : vy[c];
             vz[c] = (hit && wz) ? vz[c] + fz * dt / rbz[c] : vz[c];
+            tvx = hit ? vx[c] : tvx;
+            tvy = hit ? vy[c] : tvy;
+            tvz = hit ? vz[c] : tvz;
           }
+          // source-point trace: the velocity after the injection
+          const int ns = sd.nstep + 1;
+          sd.src_trace[it_step] = tvx;
+          sd.src_trace[ns + it_step] = tvy;
+          sd.src_trace[2 * ns + it_step] = tvz;
         }
         const long long g = (long long)k * plane + rowoff;
         st_vec(f0 + g, vx);

@@ -15,6 +15,10 @@
 - ``snapshot_bytes``: a v?%05i.bin file (:685-722): DIMX*DIMY*DIMZ values
   read at address ii + jj*NIMX + kk*NIMX*NIMY, which with the program's
   1-based cells maps each address to a cell or to never-written zeros.
+- ``recsrc_text`` / ``write_recsrc``: recsrcx.txt, recsrcy.txt, recsrcz.txt
+  of the FP64 GPU program (elatic_3d_unified_cuda_memory.cu:1202-1223): the
+  NSTEP+1 source-point values of one component, each followed by a space,
+  no newline; index 0 is the never-written 0.
 - ``read_model`` / ``write_model``: modelcp.bin, modelcs.bin, modelrh.bin,
   raw float32 (float64 in elatic_3d_unified_cuda_memory.cu), x fastest, read
   in (k, j, i) order (seismicCPML_3d_isotropic_cudazerocopy.cu:544-595).
@@ -73,6 +77,22 @@ def write_rechor(outdir: str, seis: np.ndarray, slots: np.ndarray, append: bool 
         path = os.path.join(outdir, name)
         with open(path, "a" if append else "w") as f:
             f.write(rechor_text(seis[:, c, :], slots))
+        paths.append(path)
+    return paths
+
+
+def recsrc_text(trace_comp: np.ndarray) -> str:
+    """One component of the source trace [nstep + 1] -> the file content."""
+    return "".join(_fmt(v) + " " for v in np.asarray(trace_comp).reshape(-1))
+
+
+def write_recsrc(outdir: str, trace: np.ndarray) -> list[str]:
+    """trace [3, nstep + 1] -> recsrcx.txt, recsrcy.txt, recsrcz.txt."""
+    paths = []
+    for c, name in enumerate(("recsrcx.txt", "recsrcy.txt", "recsrcz.txt")):
+        path = os.path.join(outdir, name)
+        with open(path, "w") as f:
+            f.write(recsrc_text(trace[c]))
         paths.append(path)
     return paths
 

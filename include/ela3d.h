@@ -150,6 +150,13 @@ ela3d_status ela3d_sync(ela3d_plan *plan);
 ela3d_status ela3d_get_seismograms(ela3d_plan *plan, float *out);
 ela3d_status ela3d_get_seismograms_f64(ela3d_plan *plan, double *out);
 /* Current field, compact nx*ny*nz (snapshot of simpelmodel.cpp:685-722). */
+/* Source-point trace, [3][nstep + 1]: the components the source acts on at
+ * its cell, right after each step's injection (index it = 1..nstep; index 0
+ * is 0) -- sxx syy szz for an explosive source, as the reference's FP64 GPU
+ * program records into recsrc{x,y,z}.txt
+ * (elatic_3d_unified_cuda_memory.cu:463-465,1202-1223); vx vy vz for a force. */
+ela3d_status ela3d_get_source_trace(ela3d_plan *plan, float *out);
+ela3d_status ela3d_get_source_trace_f64(ela3d_plan *plan, double *out);
 ela3d_status ela3d_get_field(ela3d_plan *plan, int32_t comp, float *out);
 ela3d_status ela3d_get_field_f64(ela3d_plan *plan, int32_t comp, double *out);
 /* Total kinetic + strain energy [J], FP64 device reduction (no counterpart
@@ -258,6 +265,7 @@ ela3d_status ela3d_batch_run(ela3d_batch *b, int32_t nsteps);
 ela3d_status ela3d_batch_run_timed(ela3d_batch *b, int32_t nsteps, double *ms);
 ela3d_status ela3d_batch_get_seismograms(ela3d_batch *b, int32_t shot, float *out);
 ela3d_status ela3d_batch_get_field(ela3d_batch *b, int32_t shot, int32_t comp, float *out);
+ela3d_status ela3d_batch_get_source_trace(ela3d_batch *b, int32_t shot, float *out);
 ela3d_status ela3d_batch_info(ela3d_batch *b, int32_t shot, ela3d_plan_info *out);
 ela3d_status ela3d_batch_destroy(ela3d_batch *b);
 

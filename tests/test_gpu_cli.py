@@ -42,3 +42,8 @@ def test_cli_files_match_reference_program(built, tmp_path):
         assert a.size == b.size == 25 * 23 * 21 and rel_l2(a, b) < 2e-5
     assert os.path.exists(os.path.join(out, "vz00010.bin"))
     assert np.load(os.path.join(out, "seis.npy")).shape == (1, 3, p.nstep // p.sampgat)
+    # source-point trace: vz at the source cell of the force source after each step
+    tz = np.array([float(v) for v in open(os.path.join(out, "recsrcz.txt")).read().split()])
+    assert tz.size == p.nstep + 1 and tz[0] == 0
+    i, j, k = p.src
+    assert abs(tz[-1] - fields[2][k, j, i]) <= 1e-4 * np.abs(fields[2]).max()

@@ -72,3 +72,28 @@ def test_too_many_receivers_rejected_like_the_reference():
 
     with pytest.raises(ValueError):
         gather_layout(20, 20, 10, 4, 2, 5)   # ylen = (20 - 20) / 2 = 0
+
+
+def test_recsrc_text_matches_cpp_iostream(tmp_path):
+    """recsrc?.txt values are printed by `fout << double << " "`
+    (elatic_3d_unified_cuda_memory.cu:1205-1223); pinned against g++."""
+    import shutil
+    import subprocess
+
+    from ela3d_gb300 import refio
+
+    if shutil.which("g++") is None:
+        pytest.skip("g++ not available")
+    vals = np.array([0.0, 1.5, -2.25e-7, 123456789.0, 3.14159265358979, 1e-300, -0.0, 7.0e5, 1234567.0,
+                     0.000123456789, -98765.4321], np.float64)
+    src = tmp_path / "w.cpp"
+    src.write_text('#include <fstream>\n#include <cstdlib>\nint main(int c, char **v) {\n'
+                   '  std::ofstream f(v[1]);\n  for (int i = 2; i < c; ++i) f << std::strtod(v[i], 0) << " ";\n}\n')
+    exe = tmp_path / "w"
+    subprocess.run(["g++", "-O1", str(src), "-o", str(exe)], check=True)
+    out = tmp_path / "recsrcx.txt"
+    subprocess.run([str(exe), str(out)] + [repr(float(v)) for v in vals], check=True)
+    assert refio.recsrc_text(vals) == out.read_text()
+    paths = refio.write_recsrc(str(tmp_path), np.stack([vals, vals * 2, vals * 3]))
+    assert [os.path.basename(q) for q in paths] == ["recsrcx.txt", "recsrcy.txt", "recsrcz.txt"]
+    assert open(paths[0]).read() == out.read_text()
