@@ -15,11 +15,14 @@ over ranks.  Also reported:
             (plan creation with the model upload, the run, the seismogram
             read-back), wall clock;
   cpu_baseline  the reference CPU program (oracle/_ref, else the oracle's C
-            restatement) on 1 core, a bounded sample of the same shot.
+            restatement) on 1 core, a bounded sample of the same shot;
+  reference_gpu_program  the reference's own FP32 CUDA program, built from
+            its source into oracle/_ref, at the same grid size on this GPU.
 Also in the same line: "batched" (64 shots of the 256^3 anticline sharing
 one model, advanced together), "uneven" (48 uneven grids together vs one
 at a time) and "serving" (a Poisson request stream swept to saturation,
-p50/p99 latency), each next to the single-shot path on the same GPU.
+p50/p99 latency), each next to the single-shot path on the same GPU, each
+with an FP64 re-run of sampled shots (fp64_check).
 Reference arm (--impl reference): the reference CPU program itself on all
 host cores (one process per core, each a bounded sample of the same shot),
 rank 0 only.
@@ -138,6 +141,32 @@ def profile_traffic(kernel: str) -> float | None:
     return None
 
 
+def fp64_check(pairs) -> dict:
+    """Accuracy of FP32 results against the FP64 build of the same kernels:
+    `pairs` is a list of (label, ShotParams, cp, cs, rho, steps, fp32
+    seismograms [nrec, 3, nsamp]); each shot is re-run alone in FP64 for the
+    same steps and the first steps // sampgat samples are compared."""
+    import ela3d_gb300 as E
+
+    rows = []
+    for label, p, cp, cs, rho, steps, s32 in pairs:
+        with E.Plan(p.with_(precision=1), cp, cs, rho) as pl:
+            pl.run(steps)
+            s64 = pl.seismograms(fp64=True)
+        n = steps // p.sampgat
+        a, b = s32[..., :n].astype(np.float64), s64[..., :n]
+        norms = np.array([np.linalg.norm(b[r]) for r in range(b.shape[0])])
+        # per receiver only where the wave has arrived (a trace of pure
+        # round-off before the first arrival has no meaningful relative error)
+        live = np.flatnonzero(norms >= 1e-3 * norms.max()) if norms.size else []
+        per = [float(np.linalg.norm(a[r] - b[r]) / norms[r]) for r in live]
+        rows.append({"shot": label, "steps": steps, "rel_l2": float(np.linalg.norm(a - b) / np.linalg.norm(b)),
+                     "max_rel_l2_per_receiver": max(per) if per else None,
+                     "receivers_with_signal": f"{len(per)} of {b.shape[0]}"})
+    return {"what": "FP32 seismograms vs the same shot re-run alone in FP64 (relative L2)", "shots": rows,
+            "max_rel_l2": max(r["rel_l2"] for r in rows) if rows else None}
+
+
 # ------------------------------------------------------------ workload --
 def workload(nstep: int = 2000):
     from ela3d_gb300 import configs
@@ -209,6 +238,39 @@ def cpu_reference_rate(p, cp, cs, rho, steps: int, procs: int) -> dict:
                       f"({'reference CPU program' if kind == 'reference' else 'C restatement'}), "
                       f"{(end - start):.1f} s wall",
             "seconds": end - start}
+
+
+def reference_gpu_rate(n: int, steps: int, warm: int) -> dict:
+    """The reference's own FP32 GPU program (seismicCPML_3d_isotropic_cudazerocopy.cu,
+    built by oracle/make_ref.py into oracle/_ref) on this GPU: an n^3 grid,
+    `warm` untimed steps, then `steps` timed by the program (file output off).
+    Its own constant medium and first-derivative-of-Gaussian source; the
+    kernels are the reference's, unchanged."""
+    exe = os.path.join(ROOT, "oracle", "_ref", "ref_gpu_f32")
+    if not os.path.exists(exe):
+        return {"value": None, "unavailable": "reference GPU program not built (oracle/_ref/ref_gpu_f32)"}
+    wd = tempfile.mkdtemp(prefix="ela3d_refgpu_")
+    try:
+        r = subprocess.run([exe, str(n), str(steps + warm), str(warm), "0"], cwd=wd, capture_output=True,
+                           text=True, timeout=600)
+    finally:
+        import shutil
+
+        shutil.rmtree(wd, ignore_errors=True)
+    for line in r.stdout.splitlines():
+        if line.startswith("ELA3D_REF_GPU"):
+            f = line.split()
+            got = dict(zip(f[1::2], f[2::2]))
+            if int(got["status"]) != 0:
+                return {"value": None, "unavailable": f"reference GPU program reported CUDA status {got['status']}"}
+            secs = float(got["seconds"])
+            return {"value": n ** 3 * int(got["steps"]) / secs / 1e9, "unit": METRIC,
+                    "ms_per_step": secs * 1e3 / int(got["steps"]),
+                    "what": f"the reference's FP32 CUDA program (seismicCPML_3d_isotropic_cudazerocopy.cu: five "
+                            f"stencil kernels per step plus gather and source, 8x8x8-thread blocks), {n}^3, "
+                            f"{warm} warm-up + {got['steps']} timed steps, wall clock around its loop, file "
+                            f"output off"}
+    return {"value": None, "unavailable": f"reference GPU program exited {r.returncode} without a timing line"}
 
 
 def _port_worker(p, cp, cs, rho, steps):
@@ -293,11 +355,18 @@ def run_ours(args, rank, world, local):
             extra["serving"] = serving(args)
 
     cpu = None
+    ref_gpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         try:
             cpu = cpu_reference_rate(p, cp, cs, rho, steps=args.cpu_steps, procs=1)
         except Exception as e:  # reported, not fatal
             cpu = {"value": None, "error": str(e)}
+        try:
+            ref_gpu = reference_gpu_rate(p.nx, steps=200, warm=10)
+            if ref_gpu.get("value"):
+                ref_gpu["ours_over_reference_gpu"] = value / ref_gpu["value"]
+        except Exception as e:  # reported, not fatal
+            ref_gpu = {"value": None, "error": str(e)}
     dist.close()
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
@@ -306,7 +375,7 @@ def run_ours(args, rank, world, local):
                 "data": "synthetic (seeded anticline model)",
                 "config": config_block(p, {"steps_timed": args.steps, "tuning": tune_info}),
                 "e2e": e2e, "gpu_launches": int(2 * args.steps * world), "roofline": roof,
-                "cpu_baseline": cpu, "clocks": clk}
+                "cpu_baseline": cpu, "reference_gpu_program": ref_gpu, "clocks": clk}
         line.update(extra)
         print(json.dumps(line), flush=True)
 
@@ -340,6 +409,10 @@ def batched_shots(args, single_value: float) -> dict:
         t_read = time.perf_counter() - t1
     g = Group(world)
     value = g.sum(cells) * args.batch_steps / (g.max(ms) / 1e3) / 1e9
+    # two shots drawn by seed, checked against FP64
+    pick = sorted(np.random.default_rng(2024).choice(len(shots), size=min(2, len(shots)), replace=False).tolist())
+    steps_run = args.warmup + args.batch_steps
+    check = fp64_check([(f"shot {q}", shots[q], cp, cs, rho, steps_run, seis[q]) for q in pick])
     bpc = bytes_per_cell(256, 256, 256, 16)["step"]
     peak, _ = measured_peaks()
     return {"workload": f"anticline_256_shots: {len(shots)} shots of 256^3 sharing one model, FP32, "
@@ -349,7 +422,7 @@ def batched_shots(args, single_value: float) -> dict:
             "ratio_vs_single_shot": value / single_value,
             "frac_of_hbm_at_142B": value * bpc / peak,
             "create_s": t_create, "readback_s": t_read,
-            "tuning": tune_info,
+            "tuning": tune_info, "fp64_check": check,
             "timing": "CUDA events around replayed 50-step graphs; model stored once"}
 
 
@@ -413,6 +486,7 @@ def serving(args) -> dict:
     rng = np.random.default_rng(7)
     capacity = None
     rows = []
+    served = {}
     for load in args.serve_loads:
         with E.Server(steps_per_round=args.serve_round) as srv:
             gaps = None
@@ -435,6 +509,8 @@ def serving(args) -> dict:
                 srv.wait(t)
             wall = time.perf_counter() - t_start
             st = srv.stats()
+            if load == 0:   # every 50th request, as served in FP32
+                served = {q: srv.read(tickets[q]) for q in range(0, len(reqs), 50)}
         thr = total / wall / 1e9
         busy = total / st["busy_seconds"] / 1e9
         if load == 0:
@@ -446,6 +522,7 @@ def serving(args) -> dict:
                      "max_latency_s": st["latency_max_s"], "rounds": st["rounds"], "failed": st["failed"]})
     sat = rows[0]
     sizes = [p.cells for p, *_ in reqs]
+    check = fp64_check([(f"request {q}", *reqs[q], reqs[q][0].nstep, s) for q, s in served.items()])
     return {"workload": f"serving stream: {len(reqs)} requests (seeded lognormal edges in [64, 384], "
                         f"{min(sizes) / 1e6:.2f}-{max(sizes) / 1e6:.1f} Mcells, t_end {args.serve_t_end} s "
                         f"each; the full stream is 2000 requests of 2 s), FP32",
@@ -453,7 +530,7 @@ def serving(args) -> dict:
             "p99_latency_s": sat["p99_latency_s"],
             "single_shot_sequential_value": alone, "single_shot_sequential_wall_value": total / alone_wall / 1e9,
             "ratio_vs_single_shot": sat["gcells_per_s_wall"] / alone,
-            "sweep": rows, "steps_per_round": args.serve_round,
+            "sweep": rows, "steps_per_round": args.serve_round, "fp64_check": check,
             "timing": "wall clock from first submission to last completion (requests submitted from host "
                       "arrays, seismograms streamed back); single-shot value = device time of each request "
                       "run alone"}

@@ -10,6 +10,7 @@ output.
 from __future__ import annotations
 
 import glob
+import shutil
 import os
 import subprocess
 import sys
@@ -88,14 +89,20 @@ def build_reference() -> list[str]:
     ref_src = os.path.join(make_ref.DEFAULT_REF_DIR, make_ref.REF_NAME)
     if os.path.exists(ref_src):
         make_ref.generate(make_ref.DEFAULT_REF_DIR)
-    outs = []
-    for v in ("f32", "f64"):
-        src = os.path.join(make_ref.OUT, f"ref_{v}.cpp")
-        exe = os.path.join(make_ref.OUT, f"ref_{v}")
+    outs, procs = [], []
+    jobs = [(os.path.join(make_ref.OUT, f"ref_{v}.cpp"), os.path.join(make_ref.OUT, f"ref_{v}"),
+             make_ref.compiler_cmd) for v in ("f32", "f64")]
+    if shutil.which("nvcc"):   # the reference's FP32 GPU program, a timing baseline
+        jobs.append((os.path.join(make_ref.OUT, "ref_gpu_f32.cu"), os.path.join(make_ref.OUT, "ref_gpu_f32"),
+                     make_ref.gpu_compiler_cmd))
+    for src, exe, cmd in jobs:
         if os.path.exists(src):
             if _newer([src, os.path.join(ORACLE_DIR, "ref_harness.h")], exe):
-                subprocess.run(make_ref.compiler_cmd(src, exe), check=True)
+                procs.append((exe, subprocess.Popen(cmd(src, exe))))
             outs.append(exe)
+    for exe, p in procs:
+        if p.wait() != 0:
+            raise RuntimeError(f"building {exe} failed")
     return outs
 
 

@@ -28,6 +28,18 @@ times so that a different reference fails loudly:
 - a float64 variant replaces ``float`` by ``double`` and the f-suffixed
   libm calls by their double versions.
 
+It also builds the reference's FP32 GPU program
+``seismicCPML_3d_isotropic_cudazerocopy.cu`` (all arrays in device memory,
+five stencil kernels per step with 10x10x10-thread blocks) as a timing
+baseline, with a patch that changes no kernel: the grid edge, step count and
+warm-up come from the command line (:488-491,:521); blocks become 8x8x8
+threads so that a 256-cell edge is covered exactly (:1361-1369; with 10 the
+last 6 cells of each axis would never be updated); the per-step receiver text
+and the snapshot files are switched off by a flag (:1385,:1423); the time
+after the warm-up steps and the launch status are printed after the loop.
+Its kernels' indices were checked by reading for cubic grids whose edge is a
+multiple of 8: every neighbour access stays inside the arrays.
+
 Usage: python oracle/make_ref.py [--ref DIR] [--no-build]
 """
 from __future__ import annotations
@@ -35,12 +47,14 @@ from __future__ import annotations
 import argparse
 import os
 import re
+import shutil
 import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
 REF_NAME = "seismicCPML_3d_isotropic_simpelmodel.cpp"
+GPU_REF_NAME = "seismicCPML_3d_isotropic_cudazerocopy.cu"
 DEFAULT_REF_DIR = "/root/reference"
 
 
@@ -132,6 +146,42 @@ def patch(src: str) -> str:
     return s
 
 
+def patch_gpu(src: str) -> str:
+    """The FP32 GPU program, made runnable at a given size without file I/O
+    in the timed loop (kernels untouched)."""
+    s = src.replace("\r\n", "\n")
+    s = _sub(s, "#include <iomanip>", "#include <iomanip>\n#include <chrono>")
+    s = _sub(s, "int main(void) {", "int main(int argc, char **argv) {\n"
+             "\tconst int ref_n = argc > 1 ? atoi(argv[1]) : 200;\n"
+             "\tconst int ref_warm = argc > 3 ? atoi(argv[3]) : 0;\n"
+             "\tconst int ref_io = argc > 4 ? atoi(argv[4]) : 1;")
+    s = _sub(s, "\tNIMX = 200;\n\tNIMY = 200;\n\tNIMZ = 200;", "\tNIMX = ref_n;\n\tNIMY = ref_n;\n\tNIMZ = ref_n;")
+    s = _sub(s, "int NSTEP = 200;", "int NSTEP = argc > 2 ? atoi(argv[2]) : 200;")
+    for ax in "xyz":
+        s = _sub(s, f"threads.{ax} = 10;", f"threads.{ax} = 8;")
+    s = _sub(s, "\tfor (int it = 1; it <= NSTEP; it++) {",
+             "\tstd::chrono::steady_clock::time_point ref_t0 = std::chrono::steady_clock::now();\n"
+             "\tfor (int it = 1; it <= NSTEP; it++) {\n"
+             "\t\tif (it == ref_warm + 1) { cudaDeviceSynchronize(); ref_t0 = std::chrono::steady_clock::now(); }")
+    s = _sub(s, "if (fmod(it, sampgat) == 0) {", "if (ref_io && fmod(it, sampgat) == 0) {")
+    s = _sub(s, "if (fmod(it, IT_OUTPUT) == 0){", "if (ref_io && fmod(it, IT_OUTPUT) == 0){")
+    s = _sub(s, "\tfree(tempvz); free(tempvy); free(tempvx);",
+             "\t{\n\t\tcudaError_t ref_e = cudaDeviceSynchronize();\n"
+             "\t\tif (ref_e == cudaSuccess) ref_e = cudaGetLastError();\n"
+             "\t\tconst double ref_s = std::chrono::duration<double>(std::chrono::steady_clock::now() - ref_t0).count();\n"
+             "\t\tprintf(\"ELA3D_REF_GPU n %d steps %d seconds %.9f status %d\\n\", NIMX, NSTEP - ref_warm, ref_s,"
+             " (int)ref_e);\n\t}\n"
+             "\tfree(tempvz); free(tempvy); free(tempvx);")
+    return s
+
+
+def gpu_compiler_cmd(src: str, exe: str) -> list[str]:
+    # 512-thread blocks: at most 128 registers a thread (the kernels' launches
+    # are not error-checked by the program, so the cap keeps every launch valid)
+    return ["nvcc", "-O3", "-gencode", "arch=compute_103a,code=sm_103a", "-maxrregcount=128", "-w",
+            "-Dsprintf_s=sprintf", "-I", OUT, src, "-o", exe]
+
+
 def to_f64(s: str) -> str:
     s = re.sub(r"\bfloat\b", "double", s)
     for f in ("expf", "powf", "logf", "sinf", "cosf"):
@@ -155,6 +205,12 @@ def generate(ref_dir: str) -> None:
         f.write(to_f64(p32))
     with open(os.path.join(OUT, "conio.h"), "w") as f:
         f.write("/* empty stand-in for the Windows console header */\n")
+    gpu = os.path.join(ref_dir, GPU_REF_NAME)
+    if os.path.exists(gpu):
+        with open(gpu, "r", encoding="latin-1") as f:
+            g = patch_gpu(f.read())
+        with open(os.path.join(OUT, "ref_gpu_f32.cu"), "w") as f:
+            f.write(g)
 
 
 def build() -> list[str]:
@@ -167,6 +223,10 @@ def build() -> list[str]:
             continue
         exe = os.path.join(OUT, f"ref_{v}")
         procs.append((exe, subprocess.Popen(compiler_cmd(src, exe))))
+    gsrc = os.path.join(OUT, "ref_gpu_f32.cu")
+    if os.path.exists(gsrc) and shutil.which("nvcc"):
+        exe = os.path.join(OUT, "ref_gpu_f32")
+        procs.append((exe, subprocess.Popen(gpu_compiler_cmd(gsrc, exe))))
     for exe, p in procs:
         if p.wait() != 0:
             raise RuntimeError(f"building {exe} failed")
