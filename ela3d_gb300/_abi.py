@@ -35,6 +35,8 @@ SIGNATURES = [
     ("ela3d_get_source_trace_f64", _c.c_int, [_P, _P]),
     ("ela3d_get_field_f64", _c.c_int, [_P, _c.c_int32, _P]),
     ("ela3d_energy", _c.c_int, [_P, _c.POINTER(_c.c_double)]),
+    ("ela3d_energy_noalloc", _c.c_int, [_P, _P, _P, _P, _c.c_int32, _c.c_int32, _c.c_int32, _c.c_int32,
+                                         _c.c_double, _c.c_double, _c.c_double, _P, _P]),
     ("ela3d_plan_info_get", _c.c_int, [_P, _P]),
     ("ela3d_set_kernel_timing", _c.c_int, [_P, _c.c_int32]),
     ("ela3d_get_kernel_timing", _c.c_int, [_P, _c.POINTER(_c.c_double), _c.POINTER(_c.c_double),

@@ -162,6 +162,21 @@ ela3d_status ela3d_get_field_f64(ela3d_plan *plan, int32_t comp, double *out);
 /* Total kinetic + strain energy [J], FP64 device reduction (no counterpart
  * in the reference; the stability monitor). */
 ela3d_status ela3d_energy(ela3d_plan *plan, double *out);
+/* The same energy of caller-owned FP32 device arrays -- fields[9] = vx vy vz
+ * sxx syy szz sxy sxz syz and the model cp cs rho, each [nz][ny][pitch_x],
+ * x fastest -- written to *out (device memory) on `stream` (a cudaStream_t;
+ * NULL = the default stream); asynchronous.  Allocates no device memory,
+ * for callers that cannot allocate where they need the number (allocator
+ * hooks, host callbacks, loops that cannot afford cudaMalloc's device
+ * synchronisation).  Its intermediate sums live in a fixed array inside the
+ * library: nz <= 16384 (a larger nz returns ELA3D_ERR_INVALID_ARG), nothing
+ * in it needs to start at zero, and calls overlapping in time on one device
+ * race for it -- serialise them.  The first call on a device looks up the
+ * array's address; when capturing work into a CUDA graph, make that first
+ * call before the capture begins.  No counterpart in the reference. */
+ela3d_status ela3d_energy_noalloc(const float *const *fields, const float *cp, const float *cs,
+                                  const float *rho, int32_t nx, int32_t ny, int32_t nz, int32_t pitch_x,
+                                  double dx, double dy, double dz, double *out, void *stream);
 ela3d_status ela3d_plan_info_get(ela3d_plan *plan, ela3d_plan_info *out);
 /* Per-kernel CUDA-event timing of subsequent launches (0 = off). */
 ela3d_status ela3d_set_kernel_timing(ela3d_plan *plan, int32_t enable);
