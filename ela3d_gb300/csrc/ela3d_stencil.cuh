@@ -169,7 +169,7 @@ __device__ __forceinline__ void produce(const Item *__restrict__ items, int2 ran
                                         Issue issue, Prefetch &prefetch, unsigned *__restrict__ err, int ctl,
                                         int lane) {
   if (ctl & CTL_WITHHOLD_LOADS) return;  // test mode: no stage is ever filled
-  long long n = 0;
+  unsigned n = 0;
   bool ok = true;
   for (int ii = range.x; ii < range.y && ok; ++ii) {
     const Item it = items[ii];
@@ -189,7 +189,7 @@ __device__ __forceinline__ void produce(const Item *__restrict__ items, int2 ran
   if (lane != 0) return;
   if (!ok) atomicOr(err, DEV_ERR_TIMEOUT);
   // the block must not exit with copies in flight
-  for (long long q = (n > NS ? n - NS : 0); q < n; ++q)
+  for (unsigned q = (n > NS ? n - NS : 0); q < n; ++q)
     mbar_wait_bounded(&full[q % NS], (uint32_t)((q / NS) & 1), 200000000ull);
 }
 
@@ -256,7 +256,7 @@ __global__ void __launch_bounds__(Geo<T, TX, TY, NS, CPT, MB>::THREADS, Geo<T, T
   const int lane = tid & 31;
   const int tx = tid % G::NTX, ty = tid / G::NTX;
   const unsigned long long wait_ns = (ctl & CTL_WITHHOLD_LOADS) ? kTestWaitLimitNs : kWaitLimitNs;
-  long long n = 0;  // index of the load holding the current plane
+  unsigned n = 0;  // index of the load holding the current plane
 
   for (int ii = range.x; ii < range.y; ++ii) {
     const Item item = items[ii];
@@ -614,7 +614,7 @@ __global__ void __launch_bounds__(Geo<T, TX, TY, NS, CPT, MB>::THREADS, Geo<T, T
   // step counter: an argument for direct launches, device memory plus an
   // offset inside a replayable CUDA graph
   if (dtick) tick += *dtick;
-  long long n = 0;
+  unsigned n = 0;
 
   for (int ii = range.x; ii < range.y; ++ii) {
     const Item item = items[ii];
@@ -637,6 +637,8 @@ __global__ void __launch_bounds__(Geo<T, TX, TY, NS, CPT, MB>::THREADS, Geo<T, T
     const bool sample = (it_step % sd.sampgat == 0) && (it_step / sd.sampgat <= sd.nsamp) && it_step > 0;
     const int samp = it_step / sd.sampgat - 1;
     const int *const rec_plane = sd.rec_plane;
+    // receivers exist in this item's planes at all (most items have none)
+    const bool item_rec = sample && rec_plane[item.k1] > rec_plane[item.k0];
     const bool src_row = sd.src_kind == 0 && y == sd.src_j && sd.src_i >= xg && sd.src_i < xg + V &&
                          it_step >= 1 && it_step <= sd.nstep;
 
@@ -716,7 +718,7 @@ __global__ void __launch_bounds__(Geo<T, TX, TY, NS, CPT, MB>::THREADS, Geo<T, T
       }
 
       int rlo = 0, rhi = 0;   // receivers of this plane
-      if (sample) {
+      if (item_rec) {
         rlo = rec_plane[k];
         rhi = rec_plane[k + 1];
       }
