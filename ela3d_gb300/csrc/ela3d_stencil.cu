@@ -31,6 +31,10 @@ static const Variant kVariants[] = {
     make_variant<float, 64, 14, 4>(),
     make_variant<float, 128, 3, 4>(),
     make_variant<float, 64, 6, 4>(),
+    // FP64 (the accuracy build; its rate on GB300 makes it compute-bound):
+    // one cell per thread keeps it free of register spills
+    make_variant<double, 32, 7, 4, 1>(),
+    make_variant<double, 32, 3, 4, 1, 2>(),
     make_variant<double, 32, 6, 3>(),
     make_variant<double, 64, 3, 4>(),
 };
