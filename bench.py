@@ -521,6 +521,18 @@ def serving(args) -> dict:
                      "p50_latency_s": st["latency_p50_s"], "p99_latency_s": st["latency_p99_s"],
                      "max_latency_s": st["latency_max_s"], "rounds": st["rounds"], "failed": st["failed"]})
     sat = rows[0]
+    # the same saturated stream with a fill target: admission in arrival
+    # order only while the running shots hold fewer cells than the target
+    with E.Server(steps_per_round=args.serve_round, fill_cells=args.serve_fill) as srv:
+        t_start = time.perf_counter()
+        tickets = [srv.submit(*r) for r in reqs]
+        for t in tickets:
+            srv.wait(t)
+        wall = time.perf_counter() - t_start
+        st = srv.stats()
+    fill_row = {"fill_cells": args.serve_fill, "gcells_per_s_wall": total / wall / 1e9,
+                "p50_latency_s": st["latency_p50_s"], "p99_latency_s": st["latency_p99_s"],
+                "max_latency_s": st["latency_max_s"], "rounds": st["rounds"]}
     sizes = [p.cells for p, *_ in reqs]
     check = fp64_check([(f"request {q}", *reqs[q], reqs[q][0].nstep, s) for q, s in served.items()])
     return {"workload": f"serving stream: {len(reqs)} requests (seeded lognormal edges in [64, 384], "
@@ -530,7 +542,8 @@ def serving(args) -> dict:
             "p99_latency_s": sat["p99_latency_s"],
             "single_shot_sequential_value": alone, "single_shot_sequential_wall_value": total / alone_wall / 1e9,
             "ratio_vs_single_shot": sat["gcells_per_s_wall"] / alone,
-            "sweep": rows, "steps_per_round": args.serve_round, "fp64_check": check,
+            "sweep": rows, "saturation_with_fill_target": fill_row, "steps_per_round": args.serve_round,
+            "fp64_check": check,
             "timing": "wall clock from first submission to last completion (requests submitted from host "
                       "arrays, seismograms streamed back); single-shot value = device time of each request "
                       "run alone"}
@@ -571,6 +584,8 @@ def main():
     ap.add_argument("--serve-count", type=int, default=64)
     ap.add_argument("--serve-t-end", type=float, default=0.25)
     ap.add_argument("--serve-round", type=int, default=50)
+    ap.add_argument("--serve-fill", type=int, default=16_000_000,
+                    help="fill target (cells) of the extra saturated serving run")
     ap.add_argument("--serve-loads", type=float, nargs="+", default=[0.0, 0.3, 0.6, 0.9],
                     help="offered load as a fraction of the measured saturation rate (0 = all at once)")
     ap.add_argument("--cpu-steps", type=int, default=20)

@@ -417,7 +417,7 @@ class Batch:
 
 class ServerConfig(ctypes.Structure):
     _fields_ = [("hbm_budget_bytes", ctypes.c_int64), ("max_active", ctypes.c_int32),
-                ("steps_per_round", ctypes.c_int32), ("precision", ctypes.c_int32), ("_pad", ctypes.c_int32),
+                ("steps_per_round", ctypes.c_int32), ("precision", ctypes.c_int32), ("fill_cells", ctypes.c_int32),
                 ("tune", Tuning)]
 
 
@@ -440,7 +440,8 @@ class Server:
     """Continuous-batching request loop (ela3d_server_*)."""
 
     def __init__(self, hbm_budget_bytes: int = 0, max_active: int = 0, steps_per_round: int = 50,
-                 precision: int = 0, variant: int = -1, schedule: int = -1, chunk: int = 0, prefetch: int = -1):
+                 precision: int = 0, variant: int = -1, schedule: int = -1, chunk: int = 0, prefetch: int = -1,
+                 fill_cells: int = 0):
         lib = load_library()
         self._lib = lib
         cfg = ServerConfig()
@@ -449,6 +450,7 @@ class Server:
         cfg.max_active = max_active
         cfg.steps_per_round = steps_per_round
         cfg.precision = precision
+        cfg.fill_cells = fill_cells
         cfg.tune = Tuning(variant, schedule, chunk, -1, prefetch)
         h = ctypes.c_void_p()
         _check(lib.ela3d_server_create(ctypes.byref(cfg), ctypes.byref(h)), "ela3d_server_create")

@@ -4,8 +4,9 @@
 //
 // A worker thread owns one engine (the batched kernels).  Each round it
 //  1. admits queued requests in arrival order while their device footprint
-//     fits the budget and a slot is free (a request larger than the whole
-//     budget is refused with ELA3D_ERR_BUSY);
+//     fits the budget, a slot is free and the running shots hold fewer cells
+//     than the fill target (a request larger than the whole budget is
+//     refused with ELA3D_ERR_BUSY);
 //  2. advances every running shot by up to `steps_per_round` time steps in
 //     one launch pair per step (shots that reach their nstep inside the
 //     round stop there);
@@ -104,6 +105,11 @@ struct ela3d_server {
       if (stop) break;
       // admission, in arrival order
       std::vector<Request *> admit;
+      double active_cells = 0.0;   // held by running and just-admitted shots
+      for (uint64_t t : running) {
+        const ela3d_params &q = reqs[t]->p;
+        active_cells += (double)q.nx * q.ny * q.nz;
+      }
       while (!queue.empty()) {
         Request &r = *reqs[queue.front()];
         if (r.cancel) {
@@ -117,9 +123,11 @@ struct ela3d_server {
           continue;
         }
         const bool slot = cfg.max_active <= 0 || (int)(running.size() + admit.size()) < cfg.max_active;
-        if (!slot || used + r.footprint > budget) break;
+        const bool fill = cfg.fill_cells <= 0 || active_cells < (double)cfg.fill_cells;
+        if (!slot || !fill || used + r.footprint > budget) break;
         queue.pop_front();
         used += r.footprint;
+        active_cells += (double)r.p.nx * r.p.ny * r.p.nz;
         admit.push_back(&r);
       }
       std::vector<Request *> cancelled;
@@ -228,6 +236,7 @@ ela3d_status ela3d_server_config_default(ela3d_server_config *c) {
   *c = ela3d_server_config{};
   c->hbm_budget_bytes = 0;
   c->max_active = 0;
+  c->fill_cells = 0;
   c->steps_per_round = 50;
   c->precision = ELA3D_FP32;
   c->tune.variant = -1;

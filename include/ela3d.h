@@ -300,7 +300,10 @@ typedef struct ela3d_server_config {
     int32_t max_active;         /* concurrent shots; 0 = no limit */
     int32_t steps_per_round;    /* time steps between admission rounds (default 50) */
     int32_t precision;          /* of every request */
-    int32_t _pad;
+    int32_t fill_cells;         /* admit (in arrival order) only while the running
+                                   shots hold fewer cells than this, so early
+                                   requests finish early once the GPU is full;
+                                   0 = no target */
     ela3d_tuning tune;
 } ela3d_server_config;
 /* Request states reported by ela3d_server_poll. */

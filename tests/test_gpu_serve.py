@@ -126,3 +126,27 @@ def test_concurrent_clients(built):
             x.join()
     for q in range(len(reqs)):
         assert np.array_equal(out[q], want[q])
+
+
+def test_fill_target_admits_in_order_and_keeps_results(built):
+    """With a fill target below one request's cells the server runs one
+    request at a time, in arrival order; results are unchanged."""
+    from ela3d_gb300 import Server
+    from ela3d_gb300._abi import REQ_DONE, REQ_RUNNING
+
+    reqs = [request(s) for s in range(80, 84)]
+    want = [alone(*r) for r in reqs]
+    with Server(steps_per_round=15, variant=0, fill_cells=1) as srv:
+        tickets = [srv.submit(*r) for r in reqs]
+        most, done_order = 0, []
+        while len(done_order) < len(tickets):
+            states = [srv.poll(t)[0] for t in tickets]
+            most = max(most, sum(s == REQ_RUNNING for s in states))
+            for q, s in enumerate(states):
+                if s == REQ_DONE and q not in done_order:
+                    done_order.append(q)
+            time.sleep(0.001)
+        for q, t in enumerate(tickets):
+            assert np.array_equal(srv.read(t), want[q]), q
+    assert most <= 1
+    assert done_order == sorted(done_order)
