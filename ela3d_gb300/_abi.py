@@ -32,6 +32,9 @@ SIGNATURES = [
     ("ela3d_get_seismograms_f64", _c.c_int, [_P, _P]),
     ("ela3d_get_field", _c.c_int, [_P, _c.c_int32, _P]),
     ("ela3d_get_source_trace", _c.c_int, [_P, _P]),
+    ("ela3d_checkpoint_size", _c.c_int, [_P, _c.POINTER(_c.c_int64)]),
+    ("ela3d_checkpoint_save", _c.c_int, [_P, _P, _c.c_int64]),
+    ("ela3d_checkpoint_load", _c.c_int, [_P, _P, _c.c_int64]),
     ("ela3d_get_source_trace_f64", _c.c_int, [_P, _P]),
     ("ela3d_get_field_f64", _c.c_int, [_P, _c.c_int32, _P]),
     ("ela3d_energy", _c.c_int, [_P, _c.POINTER(_c.c_double)]),
@@ -269,6 +272,19 @@ class Plan:
             fn = self._lib.ela3d_get_seismograms_f64 if fp64 else self._lib.ela3d_get_seismograms
             _check(fn(self._h, _ptr(out)), "ela3d_get_seismograms")
         return out
+
+    def checkpoint(self) -> np.ndarray:
+        """The plan's complete state (ela3d_checkpoint_save) as a uint8 array."""
+        n = ctypes.c_int64()
+        _check(self._lib.ela3d_checkpoint_size(self._h, ctypes.byref(n)), "ela3d_checkpoint_size")
+        buf = np.empty(n.value, np.uint8)
+        _check(self._lib.ela3d_checkpoint_save(self._h, _ptr(buf), n.value), "ela3d_checkpoint_save")
+        return buf
+
+    def restore(self, buf: np.ndarray) -> None:
+        """Continue from a checkpoint of a plan with the same parameters."""
+        buf = np.ascontiguousarray(buf, np.uint8)
+        _check(self._lib.ela3d_checkpoint_load(self._h, _ptr(buf), buf.size), "ela3d_checkpoint_load")
 
     def source_trace(self, fp64: bool = False) -> np.ndarray:
         """[3, nstep + 1]: the source cell's injected components after each

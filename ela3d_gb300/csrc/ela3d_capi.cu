@@ -267,6 +267,22 @@ ela3d_status ela3d_get_seismograms_f64(ela3d_plan *plan, double *out) {
   return plan->eng->seismograms(0, out, 1);
 }
 
+ela3d_status ela3d_checkpoint_size(ela3d_plan *plan, int64_t *bytes) {
+  if (!plan || !bytes) return ELA3D_ERR_INVALID_ARG;
+  *bytes = plan->eng->checkpoint_bytes();
+  return *bytes > 0 ? ELA3D_OK : ELA3D_ERR_INVALID_ARG;
+}
+
+ela3d_status ela3d_checkpoint_save(ela3d_plan *plan, void *buf, int64_t bytes) {
+  if (!plan || !buf) return ELA3D_ERR_INVALID_ARG;
+  return plan->eng->checkpoint_save(buf, bytes);
+}
+
+ela3d_status ela3d_checkpoint_load(ela3d_plan *plan, const void *buf, int64_t bytes) {
+  if (!plan || !buf) return ELA3D_ERR_INVALID_ARG;
+  return plan->eng->checkpoint_load(buf, bytes);
+}
+
 ela3d_status ela3d_get_source_trace(ela3d_plan *plan, float *out) {
   if (!plan || !out) return ELA3D_ERR_INVALID_ARG;
   return plan->eng->source_trace(0, out, 0);

@@ -843,6 +843,65 @@ class Engine final : public EngineBase {
     return ELA3D_OK;
   }
 
+  struct CheckpointHeader {
+    char magic[8];          // "ELA3DCK1"
+    int32_t version, precision, nx, ny, nz, npml, nstep, nrec, sampgat, pml_mode, step, _pad;
+    int64_t pool_bytes;
+    double e_ref;
+  };
+
+  int64_t checkpoint_bytes() const override {
+    if (shots_.size() != 1) return -1;
+    return (int64_t)sizeof(CheckpointHeader) + (int64_t)shots_[0]->pool_bytes;
+  }
+
+  CheckpointHeader checkpoint_header() const {
+    const Shot<T> &s = *shots_[0];
+    CheckpointHeader h{};
+    std::memcpy(h.magic, "ELA3DCK1", 8);
+    h.version = 1;
+    h.precision = sizeof(T) == 8 ? ELA3D_FP64 : ELA3D_FP32;
+    h.nx = s.p.nx; h.ny = s.p.ny; h.nz = s.p.nz;
+    h.npml = s.p.npml; h.nstep = s.p.nstep; h.nrec = s.p.nrec; h.sampgat = s.p.sampgat;
+    h.pml_mode = s.p.pml_mode;
+    h.step = tick_ - s.d.tick0;
+    h.pool_bytes = (int64_t)s.pool_bytes;
+    h.e_ref = s.e_ref;
+    return h;
+  }
+
+  ela3d_status checkpoint_save(void *buf, int64_t bytes) override {
+    if (shots_.size() != 1) BAD("checkpoints hold single-shot plans");
+    if (!buf || bytes < checkpoint_bytes()) BAD("checkpoint buffer too small");
+    const CheckpointHeader h = checkpoint_header();
+    CK(cudaStreamSynchronize(stream_));
+    std::memcpy(buf, &h, sizeof h);
+    CK(cudaMemcpy(static_cast<char *>(buf) + sizeof h, shots_[0]->pool, shots_[0]->pool_bytes,
+                  cudaMemcpyDeviceToHost));
+    return ELA3D_OK;
+  }
+
+  ela3d_status checkpoint_load(const void *buf, int64_t bytes) override {
+    if (shots_.size() != 1) BAD("checkpoints hold single-shot plans");
+    if (!buf || bytes < (int64_t)sizeof(CheckpointHeader)) BAD("checkpoint buffer too small");
+    CheckpointHeader h;
+    std::memcpy(&h, buf, sizeof h);
+    const CheckpointHeader mine = checkpoint_header();
+    if (std::memcmp(h.magic, mine.magic, 8) != 0 || h.version != mine.version) BAD("not an ela3d checkpoint");
+    if (h.precision != mine.precision || h.nx != mine.nx || h.ny != mine.ny || h.nz != mine.nz ||
+        h.npml != mine.npml || h.nstep != mine.nstep || h.nrec != mine.nrec || h.sampgat != mine.sampgat ||
+        h.pml_mode != mine.pml_mode || h.pool_bytes != mine.pool_bytes)
+      BAD("checkpoint was written by a plan with other parameters");
+    if (bytes < (int64_t)sizeof h + h.pool_bytes) BAD("checkpoint buffer truncated");
+    if (h.step < 0) BAD("checkpoint step out of range");
+    Shot<T> &s = *shots_[0];
+    CK(cudaStreamSynchronize(stream_));
+    CK(cudaMemcpy(s.pool, static_cast<const char *>(buf) + sizeof h, s.pool_bytes, cudaMemcpyHostToDevice));
+    tick_ = s.d.tick0 + h.step;
+    s.e_ref = h.e_ref;
+    return ELA3D_OK;
+  }
+
   ela3d_status field(int shot, int comp, void *out, int out_fp64) override {
     if (shot < 0 || shot >= nshots() || !out) BAD("bad shot or output");
     if (comp < 0 || comp > 8) BAD("bad field component");

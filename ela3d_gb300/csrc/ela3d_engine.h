@@ -79,6 +79,12 @@ class EngineBase {
   virtual ela3d_status seismograms(int shot, void *out, int out_fp64) = 0;
   virtual ela3d_status field(int shot, int comp, void *out, int out_fp64) = 0;
   virtual ela3d_status source_trace(int shot, void *out, int out_fp64) = 0;
+  // Checkpoint of a single-shot engine: a header and the shot's whole device
+  // pool (fields, model, C-PML memory variables, traces), restorable into an
+  // engine created with the same parameters.
+  virtual int64_t checkpoint_bytes() const = 0;
+  virtual ela3d_status checkpoint_save(void *buf, int64_t bytes) = 0;
+  virtual ela3d_status checkpoint_load(const void *buf, int64_t bytes) = 0;
   virtual ela3d_status energy(int shot, double *out) = 0;
   virtual ela3d_status info(int shot, ela3d_plan_info *out) = 0;
   virtual ela3d_status set_timing(bool on) = 0;

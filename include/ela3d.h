@@ -178,6 +178,16 @@ ela3d_status ela3d_energy_noalloc(const float *const *fields, const float *cp, c
                                   const float *rho, int32_t nx, int32_t ny, int32_t nz, int32_t pitch_x,
                                   double dx, double dy, double dz, double *out, void *stream);
 ela3d_status ela3d_plan_info_get(ela3d_plan *plan, ela3d_plan_info *out);
+/* Checkpoint / resume: the plan's complete time-stepping state (the nine
+ * fields, the C-PML memory variables, the model, the seismograms and source
+ * trace so far, the step count) as one host buffer of
+ * ela3d_checkpoint_size bytes.  ela3d_checkpoint_load restores it into a
+ * plan created with the same parameters (in this process or another), which
+ * then continues exactly as the saved plan would have.  The reference's
+ * snapshots hold vx, vy, vz only and cannot resume a run; no counterpart. */
+ela3d_status ela3d_checkpoint_size(ela3d_plan *plan, int64_t *bytes);
+ela3d_status ela3d_checkpoint_save(ela3d_plan *plan, void *buf, int64_t bytes);
+ela3d_status ela3d_checkpoint_load(ela3d_plan *plan, const void *buf, int64_t bytes);
 /* Per-kernel CUDA-event timing of subsequent launches (0 = off). */
 ela3d_status ela3d_set_kernel_timing(ela3d_plan *plan, int32_t enable);
 /* Sums since timing was enabled: stress and velocity kernel milliseconds
