@@ -46,6 +46,7 @@ SIGNATURES = [
                                            _c.POINTER(_c.c_int64), _c.POINTER(_c.c_int64)]),
     ("ela3d_plan_destroy", _c.c_int, [_P]),
     ("ela3d_plan_inject_timeout", _c.c_int, [_P, _c.c_int32]),
+    ("ela3d_plan_poison_padding", _c.c_int, [_P, _c.c_double]),
     ("ela3d_select_device", _c.c_int, [_c.c_int32]),
     ("ela3d_run_timed", _c.c_int, [_P, _c.c_int32, _c.POINTER(_c.c_double)]),
     ("ela3d_slab_extent", _c.c_int, [_P, _P, _c.c_int32, _c.POINTER(_c.c_int32), _c.POINTER(_c.c_int32)]),
@@ -320,6 +321,11 @@ class Plan:
         _check(self._lib.ela3d_get_kernel_timing(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(na),
                                                  ctypes.byref(nb)), "ela3d_get_kernel_timing")
         return a.value, b.value, na.value, nb.value
+
+    def poison_padding(self, value: float = float("nan")) -> None:
+        """Test hook: `value` into every padding column of the fields and
+        memory variables (ela3d_plan_poison_padding)."""
+        _check(self._lib.ela3d_plan_poison_padding(self._h, value), "ela3d_plan_poison_padding")
 
     def inject_timeout(self, launches: int) -> None:
         """Test hook: the next `launches` kernel launches withhold their loads

@@ -324,6 +324,11 @@ ela3d_status ela3d_get_kernel_timing(ela3d_plan *plan, double *stress_ms, double
   return plan->eng->timing(stress_ms, velocity_ms, stress_launches, velocity_launches);
 }
 
+ela3d_status ela3d_plan_poison_padding(ela3d_plan *plan, double value) {
+  if (!plan) return ELA3D_ERR_INVALID_ARG;
+  return plan->eng->poison_padding(value);
+}
+
 ela3d_status ela3d_plan_inject_timeout(ela3d_plan *plan, int32_t launches) {
   if (!plan) return ELA3D_ERR_INVALID_ARG;
   return plan->eng->inject_timeout(launches);

@@ -947,6 +947,33 @@ class Engine final : public EngineBase {
     return ELA3D_OK;
   }
 
+  // Fills the padding columns [nx, px) of every field and memory-variable
+  // array of every shot with `value` (test hook).
+  ela3d_status poison_padding(double value) override {
+    CK(cudaStreamSynchronize(stream_));
+    for (auto &sp : shots_) {
+      const ShotDesc<T> &d = sp->d;
+      const int w = d.px - d.nx;
+      if (w <= 0) continue;
+      auto put = [&](T *dst, size_t dpitch, int width, size_t rows) -> cudaError_t {
+        if (width <= 0 || rows == 0) return cudaSuccess;
+        std::vector<T> fill((size_t)width * rows, (T)value);
+        return cudaMemcpy2D(dst, dpitch * sizeof(T), fill.data(), width * sizeof(T), width * sizeof(T), rows,
+                            cudaMemcpyHostToDevice);
+      };
+      const size_t rows = (size_t)d.ny * d.nz;
+      for (int c = 0; c < 9; ++c) CK(put(d.f[c] + d.nx, d.px, w, rows));
+      for (int v = 0; v < 6; ++v) {
+        CK(put(d.psi_y + v * d.psy + d.nx, d.px, w, (size_t)d.nz * d.yw));
+        CK(put(d.psi_z + v * d.psz + d.nx, d.px, w, (size_t)d.zw * d.ny));
+        // x slab: a column x >= xr sits at slab index xl + (x - xr)
+        const int x0 = std::max(d.nx, d.xr);
+        if (d.xw > 0 && x0 < d.px) CK(put(d.psi_x + v * d.psx + d.xl + (x0 - d.xr), d.xw, d.px - x0, rows));
+      }
+    }
+    return ELA3D_OK;
+  }
+
   ela3d_status inject_timeout(int launches) override {
     if (launches < 0) BAD("launches must be >= 0");
     inject_ = launches;

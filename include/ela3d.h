@@ -201,6 +201,10 @@ ela3d_status ela3d_plan_destroy(ela3d_plan *plan);
  * ELA3D_ERR_TIMEOUT.  Nothing faults or hangs; the CUDA context stays usable,
  * the plan's fields are left partly updated.  No reference counterpart. */
 ela3d_status ela3d_plan_inject_timeout(ela3d_plan *plan, int32_t steps);
+/* Test hook: writes `value` (e.g. NaN) into every padding column
+ * x in [nx, pitch_x) of the nine fields and of the C-PML memory-variable
+ * arrays -- cells no update may read into the grid.  No counterpart. */
+ela3d_status ela3d_plan_poison_padding(ela3d_plan *plan, double value);
 
 /* ---- kernel variants and tuning ----------------------------------------- */
 /* A compiled instance of the stress/velocity kernel pair: real type, x-y
