@@ -47,6 +47,7 @@ SIGNATURES = [
     ("ela3d_plan_destroy", _c.c_int, [_P]),
     ("ela3d_plan_inject_timeout", _c.c_int, [_P, _c.c_int32]),
     ("ela3d_plan_poison_padding", _c.c_int, [_P, _c.c_double]),
+    ("ela3d_plan_check_guards", _c.c_int, [_P]),
     ("ela3d_select_device", _c.c_int, [_c.c_int32]),
     ("ela3d_run_timed", _c.c_int, [_P, _c.c_int32, _c.POINTER(_c.c_double)]),
     ("ela3d_slab_extent", _c.c_int, [_P, _P, _c.c_int32, _c.POINTER(_c.c_int32), _c.POINTER(_c.c_int32)]),
@@ -326,6 +327,11 @@ class Plan:
         """Test hook: `value` into every padding column of the fields and
         memory variables (ela3d_plan_poison_padding)."""
         _check(self._lib.ela3d_plan_poison_padding(self._h, value), "ela3d_plan_poison_padding")
+
+    def check_guards(self) -> None:
+        """Raises Ela3dError (ELA3D_ERR_CORRUPT) if a write ran past a device
+        array (guard zones are on when ELA3D_GUARD_ZONES was set at creation)."""
+        _check(self._lib.ela3d_plan_check_guards(self._h), "ela3d_plan_check_guards")
 
     def inject_timeout(self, launches: int) -> None:
         """Test hook: the next `launches` kernel launches withhold their loads

@@ -39,6 +39,7 @@ const char *ela3d_status_string(ela3d_status s) {
     case ELA3D_ERR_CANCELLED: return "cancelled";
     case ELA3D_ERR_NOT_FOUND: return "not found";
     case ELA3D_ERR_NOT_READY: return "not ready";
+    case ELA3D_ERR_CORRUPT: return "device memory guard overwritten";
   }
   return "unknown status";
 }
@@ -322,6 +323,11 @@ ela3d_status ela3d_get_kernel_timing(ela3d_plan *plan, double *stress_ms, double
                                      int64_t *stress_launches, int64_t *velocity_launches) {
   if (!plan) return ELA3D_ERR_INVALID_ARG;
   return plan->eng->timing(stress_ms, velocity_ms, stress_launches, velocity_launches);
+}
+
+ela3d_status ela3d_plan_check_guards(ela3d_plan *plan) {
+  if (!plan) return ELA3D_ERR_INVALID_ARG;
+  return plan->eng->check_guards();
 }
 
 ela3d_status ela3d_plan_poison_padding(ela3d_plan *plan, double value) {

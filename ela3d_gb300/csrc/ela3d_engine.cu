@@ -195,6 +195,8 @@ struct Shot {
   ShotDesc<T> d{};
   ShotMaps maps{};
   double e_ref = -1.0; // energy monitor reference after the source ended
+  struct Guard { size_t off, bytes; const char *after; };
+  std::vector<Guard> guards;  // debug guard zones in the pool (empty unless enabled)
   uint64_t key = 0;    // stable identity while shots join and leave
 };
 
@@ -253,6 +255,11 @@ class Engine final : public EngineBase {
     CK(cudaMemset(d_tick_, 0, sizeof(int)));
     // ELA3D_PSI_PREFETCH=<bits> overrides the tuned prefetch mode (experiments)
     if (const char *e = std::getenv("ELA3D_PSI_PREFETCH")) prefetch_env_ = std::atoi(e) & (CTL_PF_X | CTL_PF_YZ);
+    // ELA3D_GUARD_ZONES=<bytes> (debug): guard zones around every pool array
+    if (const char *e = std::getenv("ELA3D_GUARD_ZONES")) {
+      const long long b = std::atoll(e);
+      if (b > 0) guard_ = al256((size_t)std::min(b, 1ll << 20));
+    }
     return ELA3D_OK;
   }
 
@@ -343,22 +350,41 @@ class Engine final : public EngineBase {
     const size_t cells = (size_t)px * ny * nz;
     const size_t nrec = (size_t)p.nrec;
     size_t o = 0;
-    auto take = [&](size_t bytes) { size_t at = o; o += al256(bytes); return at; };
+    // with guard zones on (debug), the pool starts with one and every array
+    // is followed by one, covering its alignment slack too
+    if (guard_) {
+      s.guards.push_back({0, guard_, "the start of the pool"});
+      o = guard_;
+    }
+    auto take = [&](size_t bytes, const char *name) {
+      const size_t at = o;
+      o += al256(bytes);
+      if (guard_) {
+        s.guards.push_back({at + bytes, o + guard_ - (at + bytes), name});
+        o += guard_;
+      }
+      return at;
+    };
+    static const char *kFieldNames[9] = {"vx", "vy", "vz", "sxx", "syy", "szz", "sxy", "sxz", "syz"};
     size_t o_f[9];
-    for (int c = 0; c < 9; ++c) o_f[c] = take(cells * sizeof(T));
+    for (int c = 0; c < 9; ++c) o_f[c] = take(cells * sizeof(T), kFieldNames[c]);
     size_t o_m[3] = {0, 0, 0};
+    static const char *kModelNames[3] = {"cp", "cs", "rho"};
     if (shared_model_of < 0)
-      for (int c = 0; c < 3; ++c) o_m[c] = take(cells * sizeof(T));
+      for (int c = 0; c < 3; ++c) o_m[c] = take(cells * sizeof(T), kModelNames[c]);
     const size_t psx = (size_t)nz * ny * xw, psy = (size_t)nz * yw * px, psz = (size_t)zw * ny * px;
-    const size_t o_px = take(6 * psx * sizeof(T)), o_py = take(6 * psy * sizeof(T)), o_pz = take(6 * psz * sizeof(T));
-    const size_t o_stf = take(std::max(1, p.nstep) * sizeof(T));
-    const size_t o_rp = take((size_t)(nz + 1) * sizeof(int));
-    const size_t o_rs = take(std::max<size_t>(1, nrec) * sizeof(int4));
-    const size_t o_seis = take(std::max<size_t>(1, nrec * 3 * s.nsamp) * sizeof(T));
-    const size_t o_trace = take(3 * (size_t)(p.nstep + 1) * sizeof(T));
+    const size_t o_px = take(6 * psx * sizeof(T), "the x-slab memory variables");
+    const size_t o_py = take(6 * psy * sizeof(T), "the y-slab memory variables");
+    const size_t o_pz = take(6 * psz * sizeof(T), "the z-slab memory variables");
+    const size_t o_stf = take(std::max(1, p.nstep) * sizeof(T), "the source time function");
+    const size_t o_rp = take((size_t)(nz + 1) * sizeof(int), "the receiver plane index");
+    const size_t o_rs = take(std::max<size_t>(1, nrec) * sizeof(int4), "the sorted receivers");
+    const size_t o_seis = take(std::max<size_t>(1, nrec * 3 * s.nsamp) * sizeof(T), "the seismograms");
+    const size_t o_trace = take(3 * (size_t)(p.nstep + 1) * sizeof(T), "the source trace");
     s.pool_bytes = o;
     CK(cudaMalloc(&s.pool, s.pool_bytes));
     CK(cudaMemsetAsync(s.pool, 0, s.pool_bytes, stream_));
+    for (const auto &g : s.guards) CK(cudaMemsetAsync(s.pool + g.off, kGuardByte, g.bytes, stream_));
 
     ShotDesc<T> &d = s.d;
     d.nx = nx; d.ny = ny; d.nz = nz; d.px = px;
@@ -974,6 +1000,24 @@ class Engine final : public EngineBase {
     return ELA3D_OK;
   }
 
+  // Verifies every guard zone of every shot still holds kGuardByte.
+  ela3d_status check_guards() override {
+    CK(cudaStreamSynchronize(stream_));
+    for (auto &sp : shots_) {
+      for (const auto &g : sp->guards) {
+        std::vector<unsigned char> h(g.bytes);
+        CK(cudaMemcpy(h.data(), sp->pool + g.off, g.bytes, cudaMemcpyDeviceToHost));
+        for (size_t i = 0; i < g.bytes; ++i)
+          if (h[i] != kGuardByte) {
+            set_last_error("guard zone after " + std::string(g.after) + " overwritten at byte " +
+                           std::to_string(i) + " of " + std::to_string(g.bytes));
+            return ELA3D_ERR_CORRUPT;
+          }
+      }
+    }
+    return ELA3D_OK;
+  }
+
   ela3d_status inject_timeout(int launches) override {
     if (launches < 0) BAD("launches must be >= 0");
     inject_ = launches;
@@ -1103,6 +1147,8 @@ class Engine final : public EngineBase {
   int inject_ = 0;   // steps left whose launches withhold their loads (test hook)
   int prefetch_ = kPrefetchDefault;  // memory-variable prefetch hints (x slab to L1, y/z slabs to L2)
   int prefetch_env_ = -1;
+  size_t guard_ = 0;   // bytes of each debug guard zone (0 = off)
+  static constexpr unsigned char kGuardByte = 0xA5;
   int *d_tick_ = nullptr;
   cudaGraphExec_t gexec_ = nullptr;
   bool use_graphs_ = true, capturing_ = false;

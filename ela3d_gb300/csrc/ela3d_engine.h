@@ -90,6 +90,7 @@ class EngineBase {
   virtual ela3d_status set_timing(bool on) = 0;
   virtual ela3d_status inject_timeout(int launches) = 0;
   virtual ela3d_status poison_padding(double value) = 0;
+  virtual ela3d_status check_guards() = 0;
   virtual void set_retire(bool on) = 0;
   // live composition (serving): shots may join after finalize and leave
   virtual uint64_t last_key() const = 0;  // key of the most recently added shot

@@ -41,7 +41,8 @@ typedef enum ela3d_status {
     ELA3D_ERR_BUSY = 7,       /* admission refused: not enough device memory / slots */
     ELA3D_ERR_CANCELLED = 8,
     ELA3D_ERR_NOT_FOUND = 9,
-    ELA3D_ERR_NOT_READY = 10
+    ELA3D_ERR_NOT_READY = 10,
+    ELA3D_ERR_CORRUPT = 11    /* a guard zone around a device array was overwritten */
 } ela3d_status;
 
 /* Arithmetic of the time loop.  FP32 is the production path; FP64 is the
@@ -205,6 +206,12 @@ ela3d_status ela3d_plan_inject_timeout(ela3d_plan *plan, int32_t steps);
  * x in [nx, pitch_x) of the nine fields and of the C-PML memory-variable
  * arrays -- cells no update may read into the grid.  No counterpart. */
 ela3d_status ela3d_plan_poison_padding(ela3d_plan *plan, double value);
+/* Debug check: with the environment variable ELA3D_GUARD_ZONES=<bytes> set
+ * when a plan is created, every array in its device pool is followed (and
+ * the pool preceded) by a zone of that many bytes filled with 0xA5; this
+ * call verifies every zone is intact (ELA3D_ERR_CORRUPT names the array a
+ * write ran past).  OK when guard zones are off.  No counterpart. */
+ela3d_status ela3d_plan_check_guards(ela3d_plan *plan);
 
 /* ---- kernel variants and tuning ----------------------------------------- */
 /* A compiled instance of the stress/velocity kernel pair: real type, x-y

@@ -95,7 +95,7 @@ def test_status_strings(built):
     from ela3d_gb300 import _abi
 
     lib = _abi.load_library()
-    for s in range(0, 11):
+    for s in range(0, 12):
         assert lib.ela3d_status_string(s).decode() not in ("", "unknown status")
     assert lib.ela3d_status_string(99).decode() == "unknown status"
     assert lib.ela3d_version().decode().startswith("ela3d-gb300")
