@@ -105,7 +105,10 @@ ela3d_status ela3d_variant_get(int32_t index, ela3d_variant_info *out) {
 static TuneChoice resolve_tuning(const std::vector<ela3d_params> &ps, const float *const *cp,
                                  const float *const *cs, const float *const *rho, const ela3d_tuning *t) {
   const ela3d_params &p = ps[0];
-  TuneChoice c = default_choice(p.precision == ELA3D_FP64, p.nx, p.ny, p.nz);
+  // (the size-aware default applies to single shots; many shots give
+  // round-robin chunks enough to go around)
+  TuneChoice c = ps.size() == 1 ? default_choice(p.precision == ELA3D_FP64, p.nx, p.ny, p.nz)
+                                : default_choice(p.precision == ELA3D_FP64, 0, 0, 0);
   const bool explicit_variant = t && t->variant >= 0;
   if (!explicit_variant) {
     TuneChoice cached{};

@@ -134,14 +134,28 @@ void build_schedule(const std::vector<ShotShape> &shots, int tx, int ty, int kin
 }
 
 TuneChoice default_choice(int fp64, int nx, int ny, int nz) {
-  (void)nx; (void)ny; (void)nz;
   int n = 0;
   const Variant *v = variants(&n);
   // first variant of the precision (the list is ordered best first for
-  // large grids), z-chunks of 10 planes dealt round-robin, both prefetches
-  for (int i = 0; i < n; ++i)
-    if ((v[i].fp64 != 0) == (fp64 != 0)) return {i, 1, 10, 0, kPrefetchDefault};
-  return {0, 1, 10, 0, kPrefetchDefault};
+  // large grids), z-chunks of 10 planes dealt round-robin, both prefetches;
+  // a grid too small to give every SM several chunks gets equal contiguous
+  // shares instead (round-robin would leave some blocks with one chunk more)
+  int i = 0;
+  while (i < n && (v[i].fp64 != 0) != (fp64 != 0)) ++i;
+  if (i == n) i = 0;
+  TuneChoice c{i, 1, 10, 0, kPrefetchDefault};
+  if (nx > 0 && ny > 0 && nz > 0) {
+    int dev = 0, sms = 152;
+    if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const long long tiles = (long long)((nx + v[i].tx - 1) / v[i].tx) * ((ny + v[i].ty - 1) / v[i].ty);
+    const long long chunks = tiles * ((nz + c.chunk - 1) / c.chunk);
+    if (chunks < 8ll * std::max(1, sms)) c.kind = 0;
+    // a shot whose twelve arrays fit in L2 gains nothing from bringing its
+    // y/z-slab memory variables into L2 ahead of use
+    const double bytes = 12.0 * nx * ny * nz * (fp64 ? 8.0 : 4.0);
+    if (bytes < 96.0 * (1 << 20)) c.prefetch = CTL_PF_X;
+  }
+  return c;
 }
 
 // ------------------------------------------------------------ TMA maps --
