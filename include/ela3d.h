@@ -232,7 +232,8 @@ typedef struct ela3d_tuning {
     int32_t blocks_per_sm;  /* cap on resident blocks per SM, 0 = occupancy limit */
     int32_t prefetch;       /* prefetch of the C-PML memory variables by the
                                loading warp: bit 1 (2) x slab into L1, bit 2 (4)
-                               y and z slabs into L2; -1 = default (6) */
+                               y and z slabs into L2; -1 = built-in choice
+                               (6, or 2 for a shot that fits in L2) */
 } ela3d_tuning;
 
 /* Times every compiled variant with the candidate schedules on these shots
