@@ -96,7 +96,9 @@ typedef struct ela3d_params {
     const int32_t *rec;       /* nrec receiver cells (i, j, k), 0-based */
     int32_t nrec;
     int32_t precision;        /* ELA3D_FP32 / ELA3D_FP64 */
-    int32_t it_output;        /* snapshot cadence for ela3d_set_output (0 = none) */
+    int32_t it_output;        /* IT_OUTPUT, carried for the caller: snapshots are
+                                 read with ela3d_get_field between ela3d_run
+                                 calls of it_output steps (0 = none) */
     int32_t energy_every;     /* stability check cadence in steps (0 = off) */
 } ela3d_params;
 
@@ -151,6 +153,8 @@ ela3d_status ela3d_sync(ela3d_plan *plan);
 ela3d_status ela3d_get_seismograms(ela3d_plan *plan, float *out);
 ela3d_status ela3d_get_seismograms_f64(ela3d_plan *plan, double *out);
 /* Current field, compact nx*ny*nz (snapshot of simpelmodel.cpp:685-722). */
+ela3d_status ela3d_get_field(ela3d_plan *plan, int32_t comp, float *out);
+ela3d_status ela3d_get_field_f64(ela3d_plan *plan, int32_t comp, double *out);
 /* Source-point trace, [3][nstep + 1]: the components the source acts on at
  * its cell, right after each step's injection (index it = 1..nstep; index 0
  * is 0) -- sxx syy szz for an explosive source, as the reference's FP64 GPU
@@ -158,8 +162,6 @@ ela3d_status ela3d_get_seismograms_f64(ela3d_plan *plan, double *out);
  * (elatic_3d_unified_cuda_memory.cu:463-465,1202-1223); vx vy vz for a force. */
 ela3d_status ela3d_get_source_trace(ela3d_plan *plan, float *out);
 ela3d_status ela3d_get_source_trace_f64(ela3d_plan *plan, double *out);
-ela3d_status ela3d_get_field(ela3d_plan *plan, int32_t comp, float *out);
-ela3d_status ela3d_get_field_f64(ela3d_plan *plan, int32_t comp, double *out);
 /* Total kinetic + strain energy [J], FP64 device reduction (no counterpart
  * in the reference; the stability monitor). */
 ela3d_status ela3d_energy(ela3d_plan *plan, double *out);
@@ -223,8 +225,10 @@ typedef struct ela3d_variant_info {
 } ela3d_variant_info;
 
 /* Work schedule: kind 0 = equal contiguous share of (tile, plane) units per
- * block; kind 1 = z-chunks of `chunk` planes dealt round-robin.  Negative
- * fields select the built-in default. */
+ * block; kind 1 = z-chunks of `chunk` planes dealt round-robin, shot by
+ * shot; kind 2 = the same chunks interleaved across shots (blocks running
+ * together hold the same tile of different shots, so a shared model tile is
+ * read from DRAM once).  Negative fields select the built-in choice. */
 typedef struct ela3d_tuning {
     int32_t variant;        /* index < ela3d_variant_count(), or -1 */
     int32_t schedule;       /* 0, 1, 2, or -1 */
