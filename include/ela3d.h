@@ -313,7 +313,8 @@ ela3d_status ela3d_batch_destroy(ela3d_batch *b);
 /* ---- serving: continuous batching ---------------------------------------- */
 /* A request loop on one GPU.  Shot requests of any size are queued and
  * admitted in arrival order while their device footprint fits the budget
- * (and a slot is free); admitted shots stay resident and are advanced
+ * (and a slot is free, and the fill target is not reached); admitted shots
+ * stay resident and are advanced
  * together by the batched kernels, `steps_per_round` steps per round;
  * requests arriving meanwhile join at the next round, and finished shots
  * leave, freeing memory.  Seismogram samples are copied back after every
