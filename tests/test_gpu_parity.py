@@ -60,6 +60,7 @@ CASES = {
     "thin_z": {"shape": (52, 44, 14), "npml": 4},
     "pml_covers_grid": {"shape": (16, 18, 20), "npml": 9, "nstep": 60},
     "no_pml": {"npml": 0},
+    "explosive_far_corner": {"stf": 1, "src_kind": 1, "src": (0, 33, 45)},
 }
 
 
@@ -99,6 +100,30 @@ def test_variants_and_schedules_bit_identical(built):
             else:
                 assert np.array_equal(seis, ref[0]), (i, sched, chunk, pf)
                 assert np.array_equal(fields, ref[1]), (i, sched, chunk, pf)
+
+
+def test_fp64_variants_agree(built):
+    """Schedules are bit-identical within an FP64 variant; variants with one
+    and two cells per thread fuse multiply-adds differently, so across them
+    the results agree to round-off (1e-13 relative L2)."""
+    import ela3d_gb300
+
+    p, cp, cs, rho = small_case(nstep=30, precision=1)
+    ref = None
+    for i, v in enumerate(ela3d_gb300.variants()):
+        if not v.fp64:
+            continue
+        mine = None
+        for sched, chunk in ((0, 0), (1, 6)):
+            seis, fields = run_gpu(p, cp, cs, rho, variant=i, schedule=sched, chunk=chunk)
+            if mine is None:
+                mine = (seis, fields)
+            else:
+                assert np.array_equal(seis, mine[0]) and np.array_equal(fields, mine[1]), (i, sched, chunk)
+        if ref is None:
+            ref = mine
+        else:
+            assert rel_l2(mine[0], ref[0]) <= 1e-13 and rel_l2(mine[1], ref[1]) <= 1e-13, i
 
 
 def test_resume_equals_single_run(built):
