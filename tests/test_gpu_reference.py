@@ -100,6 +100,26 @@ def test_anticline_256_fp32_vs_fp64(built):
     assert max(wave) <= 1e-3
 
 
+def test_anticline_256_linear_in_the_source_amplitude(built):
+    """Full size, size-independent property: the time loop is linear and
+    homogeneous in the fields, so twice the source factor gives twice every
+    seismogram sample and field value.  Scaling by 2 is exact in floating
+    point except through gradual underflow: the wave's leading edge grows
+    out of subnormal values, whose rounding differs between the two runs and
+    is then carried along relatively, so the agreement is to round-off."""
+    from ela3d_gb300 import configs
+
+    p, cp, cs, rho = configs.anticline_256(nstep=300)
+    s1, f1 = run(p, cp, cs, rho)
+    s2, f2 = run(p.with_(factor=2 * p.factor), cp, cs, rho)
+    for a, b in ((s1, s2), (f1, f2)):
+        a2 = 2 * a.astype(np.float64)
+        assert np.abs(b).max() > 0
+        assert rel_l2(b, a2) <= 1e-6
+        assert np.abs(b - a2).max() <= 1e-5 * np.abs(b).max()
+        print(f"doubling: rel L2 {rel_l2(b, a2):.2e}, exact in {np.mean(b == a2):.1%} of values")
+
+
 def test_centred_source_symmetry(built):
     """vz from a vertical force at the centre of a homogeneous cube with the
     clean profiles is mirror-symmetric in x and y about the source (the
