@@ -689,6 +689,18 @@ class Engine final : public EngineBase {
         tick_ += seg;
         continue;
       }
+      // a composition's first kGraphSteps steps run as direct launches; the
+      // graph is captured only once it has lasted that long (a serving
+      // round whose composition never repeats pays for no capture)
+      if (use_graphs_ && !timing_ && inject_ == 0 && !gexec_ && seg >= kGraphSteps &&
+          steps_on_schedule_ < kGraphSteps) {
+        for (int d = std::min(seg, kGraphSteps - steps_on_schedule_); d > 0; --d, --seg) {
+          ela3d_status st = launch_step(tick_ + 1, nullptr);
+          if (st != ELA3D_OK) return st;
+          ++tick_;
+          ++steps_on_schedule_;
+        }
+      }
       const bool graphs = use_graphs_ && !timing_ && inject_ == 0 && seg >= kGraphSteps;
       if (graphs) {
         ela3d_status st = ensure_graph();
@@ -705,6 +717,7 @@ class Engine final : public EngineBase {
         ela3d_status st = launch_step(tick_ + 1, nullptr);
         if (st != ELA3D_OK) return st;
         ++tick_;
+        ++steps_on_schedule_;
       }
     }
     return ELA3D_OK;
@@ -770,6 +783,7 @@ class Engine final : public EngineBase {
     if (!sched_key_.empty() && key == sched_key_ && sched_valid_) return ELA3D_OK;
     sched_key_ = key;
     sched_valid_ = true;
+    steps_on_schedule_ = 0;
     invalidate_graph();
     if (shapes.empty()) {
       nblocks_ = 0;
@@ -1162,6 +1176,7 @@ class Engine final : public EngineBase {
   int prefetch_ = kPrefetchDefault;  // memory-variable prefetch hints (x slab to L1, y/z slabs to L2)
   int prefetch_env_ = -1;
   size_t guard_ = 0;   // bytes of each debug guard zone (0 = off)
+  int steps_on_schedule_ = 0;  // steps run with the current work items
   static constexpr unsigned char kGuardByte = 0xA5;
   int *d_tick_ = nullptr;
   cudaGraphExec_t gexec_ = nullptr;
