@@ -597,7 +597,8 @@ def main():
                     help="fill target (cells) of the extra saturated serving run")
     ap.add_argument("--serve-loads", type=float, nargs="+", default=[0.0, 0.3, 0.6, 0.9],
                     help="offered load as a fraction of the measured saturation rate (0 = all at once)")
-    ap.add_argument("--cpu-steps", type=int, default=20)
+    ap.add_argument("--cpu-steps", type=int, default=50,
+                    help="time steps of the one-core CPU baseline sample (about 15 s of CPU work)")
     ap.add_argument("--ref-steps-cap", type=int, default=20)
     args = ap.parse_args()
     if args.warmup < 3:
