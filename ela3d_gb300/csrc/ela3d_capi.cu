@@ -148,8 +148,10 @@ ela3d_status ela3d_plan_create_tuned(const ela3d_params *p, const float *cp, con
   plan->p = *p;
   plan->eng = make_engine(plan->fp64, &st);
   if (st == ELA3D_OK) st = plan->eng->add_shot(*p, cp, cs, rho, -1);
-  const TuneChoice c = resolve_tuning({*p}, &cp, &cs, &rho, tune);
-  if (st == ELA3D_OK) st = plan->eng->finalize(&c);
+  if (st == ELA3D_OK) {   // (tuning may time candidates: only for a valid shot)
+    const TuneChoice c = resolve_tuning({*p}, &cp, &cs, &rho, tune);
+    st = plan->eng->finalize(&c);
+  }
   if (st != ELA3D_OK) {
     delete plan;
     return st;
@@ -175,8 +177,10 @@ ela3d_status ela3d_plan_create_model(const ela3d_params *p, const ela3d_model_sp
   ModelSpec spec;
   std::memcpy(&spec, model, sizeof(spec));
   if (st == ELA3D_OK) st = plan->eng->add_shot(*p, nullptr, nullptr, nullptr, -1, &spec);
-  const TuneChoice c = resolve_tuning({*p}, nullptr, nullptr, nullptr, tune);
-  if (st == ELA3D_OK) st = plan->eng->finalize(&c);
+  if (st == ELA3D_OK) {
+    const TuneChoice c = resolve_tuning({*p}, nullptr, nullptr, nullptr, tune);
+    st = plan->eng->finalize(&c);
+  }
   if (st != ELA3D_OK) {
     delete plan;
     return st;

@@ -299,6 +299,17 @@ class Engine final : public EngineBase {
       BAD("bad model spec");
     auto sh = std::make_unique<Shot<T>>();
     Shot<T> &s = *sh;
+    // any failure below returns through CK/BAD: free what was allocated
+    struct Undo {
+      Engine *e;
+      Shot<T> *s;
+      float *stage = nullptr;
+      bool keep = false;
+      ~Undo() {
+        if (stage) cudaFree(stage);
+        if (!keep) e->release_shot(*s);
+      }
+    } undo{this, &s};
     s.p = p;
     s.rec.assign(p.rec, p.rec + 3 * (size_t)p.nrec);
     s.p.rec = s.rec.data();
@@ -452,14 +463,13 @@ class Engine final : public EngineBase {
           CK(cudaMemcpy2DAsync(dst[c], px * sizeof(T), src[c], nx * sizeof(float), nx * sizeof(float),
                                (size_t)ny * nz, cudaMemcpyHostToDevice, stream_));
       } else {
-        float *stage = nullptr;
-        CK(cudaMalloc(&stage, (size_t)nx * ny * nz * sizeof(float)));
+        CK(cudaMalloc(&undo.stage, (size_t)nx * ny * nz * sizeof(float)));
         for (int c = 0; c < 3; ++c) {
-          CK(cudaMemcpyAsync(stage, src[c], (size_t)nx * ny * nz * sizeof(float), cudaMemcpyHostToDevice, stream_));
-          CK(Fp<T>::pad(stage, dst[c], nx, ny, nz, px, stream_));
+          CK(cudaMemcpyAsync(undo.stage, src[c], (size_t)nx * ny * nz * sizeof(float), cudaMemcpyHostToDevice,
+                             stream_));
+          CK(Fp<T>::pad(undo.stage, dst[c], nx, ny, nz, px, stream_));
         }
         CK(cudaStreamSynchronize(stream_));
-        CK(cudaFree(stage));
       }
     }
     // 4. source time function (FP64 on the device)
@@ -488,6 +498,7 @@ class Engine final : public EngineBase {
       CK(cudaStreamSynchronize(stream_));
     }
     if (p.src_kind == ELA3D_SRC_EXPLOSIVE) any_explosive_ = true;
+    undo.keep = true;   // the shot is owned by the engine from here on
     shots_.push_back(std::move(sh));
     if (finalized_) {  // a shot joining a running engine
       Shot<T> &ns = *shots_.back();
