@@ -150,3 +150,21 @@ def test_fill_target_admits_in_order_and_keeps_results(built):
             assert np.array_equal(srv.read(t), want[q]), q
     assert most <= 1
     assert done_order == sorted(done_order)
+
+
+def test_fp64_requests_equal_alone(built):
+    """An FP64 server: each request's seismograms equal the FP64 shot run alone."""
+    from ela3d_gb300 import Plan, Server
+
+    reqs = [request(s, t_end=0.08) for s in range(90, 93)]
+    reqs = [(p.with_(precision=1), cp, cs, rho) for p, cp, cs, rho in reqs]
+    want = []
+    for p, cp, cs, rho in reqs:
+        with Plan(p, cp, cs, rho) as plan:
+            plan.run(p.nstep)
+            want.append(plan.seismograms())
+    with Server(steps_per_round=20, precision=1) as srv:
+        tickets = [srv.submit(*r) for r in reqs]
+        for q, t in enumerate(tickets):
+            srv.wait(t)
+            assert np.array_equal(srv.read(t), want[q]), q
