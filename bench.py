@@ -16,6 +16,8 @@ reported:
   e2e       one full 2000-step shot through the C ABI from host arrays
             (plan creation with the model upload, the run, the seismogram
             read-back), wall clock;
+  accuracy  that shot's every seismogram and final field component against
+            the FP64 build of the same kernels (relative L2);
   cpu_baseline  the reference CPU program (oracle/_ref, else the oracle's C
             restatement) on 1 core, a bounded sample of the same shot;
   reference_gpu_program  the reference's own FP32 CUDA program, built from
@@ -48,6 +50,7 @@ import numpy as np  # noqa: E402
 
 METRIC = "Gcell-updates/s"
 WORKLOAD = "anticline_256"
+FIELD_NAMES = ("vx", "vy", "vz", "sxx", "syy", "szz", "sxy", "sxz", "syz")  # ela3d_get_field order
 
 
 def log(*a):
@@ -167,6 +170,26 @@ def fp64_check(pairs) -> dict:
                      "receivers_with_signal": f"{len(per)} of {b.shape[0]}"})
     return {"what": "FP32 seismograms vs the same shot re-run alone in FP64 (relative L2)", "shots": rows,
             "max_rel_l2": max(r["rel_l2"] for r in rows) if rows else None}
+
+
+def shot_accuracy(p, cp, cs, rho, seis32, fields32) -> dict:
+    """Relative L2 error of every seismogram (one receiver's vx, vy, vz
+    record, wherever the FP64 record is not all zero) and of each final
+    field component of the FP32 shot against the FP64 build run on the same
+    inputs for the same steps."""
+    import ela3d_gb300 as E
+
+    with E.Plan(p.with_(precision=1), cp, cs, rho) as pl:
+        pl.run(p.nstep)
+        s64 = pl.seismograms(fp64=True)
+        f64 = [pl.field(c, fp64=True) for c in range(9)]
+    rel = lambda a, b: float(np.linalg.norm(a.astype(np.float64) - b) / np.linalg.norm(b))  # noqa: E731
+    per = [rel(seis32[r], s64[r]) for r in range(s64.shape[0]) if np.any(s64[r])]
+    wave = {name: rel(a, b) for name, a, b in zip(FIELD_NAMES, fields32, f64) if np.any(b)}
+    return {"what": f"FP32 shot vs the FP64 build, {p.nstep} steps (relative L2)",
+            "max_rel_l2_per_seismogram": max(per) if per else None, "seismograms": len(per),
+            "rel_l2_all_seismograms": rel(seis32, s64), "final_wavefield_rel_l2": wave,
+            "max_final_wavefield_rel_l2": max(wave.values()) if wave else None}
 
 
 # ------------------------------------------------------------ workload --
@@ -324,18 +347,22 @@ def run_ours(args, rank, world, local):
 
     # e2e: one whole shot through the C ABI from host arrays
     e2e = None
+    accuracy = None
     if not args.no_e2e:
         dist.barrier()
         t0 = time.perf_counter()
-        with E.Plan(p, cp, cs, rho, **tune) as shot:
-            shot.run(p.nstep)
-            seis = shot.seismograms()
+        shot = E.Plan(p, cp, cs, rho, **tune)
+        shot.run(p.nstep)
+        seis = shot.seismograms()
         t_e2e = dist.max(time.perf_counter() - t0)
         e2e = {"value": cells * p.nstep * world / t_e2e / 1e9, "unit": METRIC,
                "h2d_bytes_per_step": int(3 * cells * 4 / p.nstep),
                "d2h_bytes_per_step": int(seis.nbytes / p.nstep),
                "what": f"full {p.nstep}-step shot: plan creation with model upload, run, seismogram read-back",
                "seconds": t_e2e}
+        if rank == 0 and not args.no_accuracy:
+            accuracy = shot_accuracy(p, cp, cs, rho, seis, [shot.field(c) for c in range(9)])
+        shot.close()
     clk = clocks.stop()
 
     bpc = bytes_per_cell(p.nx, p.ny, p.nz, p.npml)
@@ -382,7 +409,7 @@ def run_ours(args, rank, world, local):
                 "data": "synthetic (seeded anticline model)",
                 "config": config_block(p, {"steps_timed": args.steps, "tuning": tune_info}),
                 "e2e": e2e, "gpu_launches": int(launches * world), "roofline": roof,
-                "cpu_baseline": cpu, "reference_gpu_program": ref_gpu, "clocks": clk}
+                "cpu_baseline": cpu, "reference_gpu_program": ref_gpu, "clocks": clk, "accuracy": accuracy}
         line.update(extra)
         print(json.dumps(line), flush=True)
 
@@ -580,6 +607,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end shot (short profiling runs)")
+    ap.add_argument("--no-accuracy", action="store_true",
+                    help="skip the FP64 re-run of the end-to-end shot (accuracy of every seismogram and field)")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched and uneven workloads")
     ap.add_argument("--no-autotune", action="store_true", help="use the built-in kernel choice")
     ap.add_argument("--batch-shots", type=int, default=64)
