@@ -81,16 +81,20 @@ class ClockSampler:
     def __init__(self, device: int):
         self.device = device
         self.proc = None
-        self.path = tempfile.mktemp(prefix="ela3d_clocks_", suffix=".csv")
+        self.path = None
 
     def start(self):
         try:
-            self.fh = open(self.path, "w")
+            fd, self.path = tempfile.mkstemp(prefix="ela3d_clocks_", suffix=".csv")
+            self.fh = os.fdopen(fd, "w")
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
                                           "--format=csv,noheader,nounits", "-lms", "200"],
                                          stdout=self.fh, stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
+            if self.path:
+                self.fh.close()
+                os.unlink(self.path)
 
     def stop(self) -> dict:
         if not self.proc:
