@@ -20,6 +20,28 @@ struct ela3d_batch {
   int fp64 = 0;
 };
 
+// A caller's tuning fields, checked before any device work: -1 (0 for the
+// chunk) selects the default; a variant must exist in this build and match
+// the shots' precision.
+ela3d_status ela3d::validate_tuning(const ela3d_tuning *t, int32_t precision) {
+  if (!t) return ELA3D_OK;
+  int nv = 0;
+  const Variant *vs = variants(&nv);
+  if (t->variant >= nv || t->variant < -1) {
+    set_last_error("no such kernel variant");
+    return ELA3D_ERR_INVALID_ARG;
+  }
+  if (t->variant >= 0 && (vs[t->variant].fp64 != 0) != (precision == ELA3D_FP64)) {
+    set_last_error("kernel variant of the other precision");
+    return ELA3D_ERR_INVALID_ARG;
+  }
+  if (t->schedule < -1 || t->schedule > 2 || t->chunk < 0 || t->blocks_per_sm < -1 || t->prefetch < -1) {
+    set_last_error("tuning field out of range");
+    return ELA3D_ERR_INVALID_ARG;
+  }
+  return ELA3D_OK;
+}
+
 extern "C" {
 
 const char *ela3d_version(void) { return "ela3d-gb300 0.1"; }
@@ -137,6 +159,7 @@ ela3d_status ela3d_plan_create_tuned(const ela3d_params *p, const float *cp, con
   if (!p || !out) return ELA3D_ERR_INVALID_ARG;
   *out = nullptr;
   ela3d_status st = validate_params(*p);
+  if (st == ELA3D_OK) st = validate_tuning(tune, p->precision);
   if (st != ELA3D_OK) return st;
   if (!cp || !cs || !rho) {
     set_last_error("model arrays missing");
@@ -168,6 +191,7 @@ ela3d_status ela3d_plan_create_model(const ela3d_params *p, const ela3d_model_sp
   if (!p || !model || !out) return ELA3D_ERR_INVALID_ARG;
   *out = nullptr;
   ela3d_status st = validate_params(*p);
+  if (st == ELA3D_OK) st = validate_tuning(tune, p->precision);
   if (st != ELA3D_OK) return st;
   ela3d_plan *plan = new (std::nothrow) ela3d_plan();
   if (!plan) return ELA3D_ERR_OOM;
@@ -407,6 +431,7 @@ ela3d_status ela3d_batch_create(int32_t nshots, const ela3d_params *params, cons
       return ELA3D_ERR_INVALID_ARG;
     }
   }
+  if (validate_tuning(tune, params[0].precision) != ELA3D_OK) return ELA3D_ERR_INVALID_ARG;
   ela3d_batch *b = new (std::nothrow) ela3d_batch();
   if (!b) return ELA3D_ERR_OOM;
   b->fp64 = params[0].precision == ELA3D_FP64;

@@ -22,6 +22,8 @@ ela3d_status status_from_cuda(cudaError_t e, const char *what);
 
 // Validates a parameter block (grid, spacing, source, receivers).
 ela3d_status validate_params(const ela3d_params &p);
+// A caller's tuning fields (null = all defaults) for shots of `precision`.
+ela3d_status validate_tuning(const ela3d_tuning *t, int32_t precision);
 
 // Slab extents of one axis from its profile arrays: cells [0, lo) and
 // [hi, n) may have a != 0; every cell in [lo, hi) has a == 0 in both the

@@ -251,6 +251,7 @@ ela3d_status ela3d_server_create(const ela3d_server_config *cfg, ela3d_server **
   if (!cfg || !out) return ELA3D_ERR_INVALID_ARG;
   *out = nullptr;
   if (cfg->precision != ELA3D_FP32 && cfg->precision != ELA3D_FP64) return ELA3D_ERR_INVALID_ARG;
+  if (validate_tuning(&cfg->tune, cfg->precision) != ELA3D_OK) return ELA3D_ERR_INVALID_ARG;
   ela3d_server *s = new (std::nothrow) ela3d_server();
   if (!s) return ELA3D_ERR_OOM;
   s->cfg = *cfg;

@@ -4,6 +4,7 @@
 // per workload shape.  Results live in a process-wide cache that plan and
 // batch creation consult; ELA3D_TUNE_CACHE=<file> persists it across
 // processes and ELA3D_AUTOTUNE=1 tunes on a cache miss at creation.
+#include <algorithm>
 #include <cstdio>
 #include <cstdlib>
 #include <map>
@@ -78,12 +79,22 @@ std::string tune_key(const std::vector<ela3d_params> &ps) {
   return k.str();
 }
 
+// A cached choice is used only if this build can run it (a cache file may
+// come from a build with other variants); otherwise it counts as a miss.
 bool tune_lookup(const std::vector<ela3d_params> &ps, TuneChoice *out) {
   std::lock_guard<std::mutex> g(g_mu);
   load_locked();
   auto it = g_cache.find(tune_key(ps));
   if (it == g_cache.end()) return false;
-  *out = it->second;
+  const TuneChoice &c = it->second;
+  int nv = 0;
+  const Variant *vs = variants(&nv);
+  const bool fp64 = !ps.empty() && ps[0].precision == ELA3D_FP64;
+  if (c.variant < 0 || c.variant >= nv || (vs[c.variant].fp64 != 0) != fp64 || c.kind < 0 || c.kind > 2 ||
+      c.chunk < 0 || c.blocks_per_sm < 0)
+    return false;
+  *out = c;
+  out->prefetch &= CTL_PF_X | CTL_PF_YZ;
   return true;
 }
 

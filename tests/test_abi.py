@@ -126,6 +126,38 @@ def test_invalid_arguments_rejected_before_device(built, name):
     assert e.value.status == 1, e.value  # ELA3D_ERR_INVALID_ARG
 
 
+def _fp64_variant():
+    import ela3d_gb300
+
+    return next(i for i, v in enumerate(ela3d_gb300.variants()) if v.fp64)
+
+
+BAD_TUNING = {
+    "no_such_variant": lambda: {"variant": 10_000},
+    "variant_of_other_precision": lambda: {"variant": _fp64_variant()},
+    "schedule_kind": lambda: {"schedule": 3},
+    "negative_chunk": lambda: {"chunk": -2},
+}
+
+
+@pytest.mark.parametrize("name", sorted(BAD_TUNING))
+def test_invalid_tuning_rejected_before_device(built, name):
+    """Tuning fields are checked with the parameters, before any device work
+    (plans, generated-model plans, batches, servers)."""
+    from ela3d_gb300 import Batch, Ela3dError, Plan, Server, ShotParams
+
+    p = ShotParams(nx=20, ny=20, nz=20, nstep=10, npml=4, src=(10, 10, 10))
+    m = np.ones(p.cells, np.float32)
+    tune = BAD_TUNING[name]()
+    for make in (lambda: Plan(p, m * 3000, m * 1700, m * 2000, **tune),
+                 lambda: Plan.from_model(p, {"kind": 0, "cp0": 3000.0, "cs0": 1700.0, "rho0": 2000.0}, **tune),
+                 lambda: Batch([(p, m * 3000, m * 1700, m * 2000)], **tune),
+                 lambda: Server(**tune)):
+        with pytest.raises(Ela3dError) as e:
+            make()
+        assert e.value.status == 1, e.value  # ELA3D_ERR_INVALID_ARG
+
+
 def test_variants_listed(built):
     import ela3d_gb300
 

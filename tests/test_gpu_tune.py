@@ -36,3 +36,48 @@ def test_autotune_batch_includes_interleaved_schedules(built):
     n32 = sum(1 for v in E.variants() if not v.fp64)
     assert cand == n32 * 18         # nine schedules x two prefetch modes for a batch
     assert best.schedule in (0, 1, 2)
+
+
+CHILD = r"""
+import sys
+sys.path.insert(0, sys.argv[1])
+import numpy as np
+from ela3d_gb300 import Plan, ShotParams, media
+p = ShotParams(nx=40, ny=36, nz=44, nstep=20, npml=8, src=(20, 18, 20), rec=np.array([[10, 18, 20]], np.int32))
+cp, cs, rho = media.anticline_layers(40, 36, 44, depths=(10, 20, 30, 60), amp=4, sigma=8, seed=0)
+with Plan(p, cp, cs, rho) as a:
+    a.run(p.nstep)
+    np.save(sys.argv[2], a.seismograms())
+"""
+
+
+def test_cache_entry_this_build_cannot_run_is_ignored(built, tmp_path):
+    """A tuning cache file written by another build (a variant index this
+    build lacks, a schedule kind it does not know) counts as a miss: the plan
+    is created with the built-in choice instead of failing."""
+    import os
+    import subprocess
+    import sys
+
+    from ela3d_gb300 import Plan, ShotParams, media
+
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    cache = tmp_path / "tune.txt"
+    cache.write_text("0:1:40x36x44p8*1, 999 1 10 0 6\n")
+    prog = tmp_path / "child.py"
+    prog.write_text(CHILD)
+    out = tmp_path / "seis.npy"
+    env = dict(os.environ, ELA3D_TUNE_CACHE=str(cache))
+    env.pop("ELA3D_AUTOTUNE", None)
+    r = subprocess.run([sys.executable, str(prog), root, str(out)], env=env, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    p = ShotParams(nx=40, ny=36, nz=44, nstep=20, npml=8, src=(20, 18, 20), rec=np.array([[10, 18, 20]], np.int32))
+    cp, cs, rho = media.anticline_layers(40, 36, 44, depths=(10, 20, 30, 60), amp=4, sigma=8, seed=0)
+    with Plan(p, cp, cs, rho) as a:
+        a.run(p.nstep)
+        want = a.seismograms()
+    assert np.array_equal(np.load(out), want)
+    cache.write_text("0:1:40x36x44p8*1, 0 7 10 0 6\n")
+    r = subprocess.run([sys.executable, str(prog), root, str(out)], env=env, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    assert np.array_equal(np.load(out), want)
