@@ -228,12 +228,14 @@ typedef struct ela3d_variant_info {
  * block; kind 1 = z-chunks of `chunk` planes dealt round-robin, shot by
  * shot; kind 2 = the same chunks interleaved across shots (blocks running
  * together hold the same tile of different shots, so a shared model tile is
- * read from DRAM once).  Negative fields select the built-in choice. */
+ * read from DRAM once).  -1 (chunk: 0) selects the built-in choice; a
+ * field out of range or a variant of the other precision is
+ * ELA3D_ERR_INVALID_ARG, reported before any device work. */
 typedef struct ela3d_tuning {
     int32_t variant;        /* index < ela3d_variant_count(), or -1 */
     int32_t schedule;       /* 0, 1, 2, or -1 */
-    int32_t chunk;          /* planes per z-chunk for schedules 1 and 2 */
-    int32_t blocks_per_sm;  /* cap on resident blocks per SM, 0 = occupancy limit */
+    int32_t chunk;          /* planes per z-chunk for schedules 1 and 2, or 0 */
+    int32_t blocks_per_sm;  /* cap on resident blocks per SM, 0 = occupancy limit, -1 */
     int32_t prefetch;       /* prefetch of the C-PML memory variables by the
                                loading warp: bit 1 (2) x slab into L1, bit 2 (4)
                                y and z slabs into L2; -1 = built-in choice
