@@ -913,7 +913,27 @@ class Engine final : public EngineBase {
     int32_t version, precision, nx, ny, nz, npml, nstep, nrec, sampgat, pml_mode, step, _pad;
     int64_t pool_bytes;
     double e_ref;
+    uint64_t params_hash;   // every parameter the time loop depends on
   };
+
+  // FNV-1a over the values (not the padding) of the parameters that shape
+  // the time loop: spacings, dt, C-PML coefficients, source, receivers.  The
+  // model and fields travel in the checkpoint; the profiles and the source
+  // table are recomputed by the restoring plan from these.
+  static uint64_t params_hash(const ela3d_params &p, const std::vector<int32_t> &rec) {
+    uint64_t h = 1469598103934665603ull;
+    auto mix = [&h](const void *v, size_t n) {
+      const unsigned char *b = static_cast<const unsigned char *>(v);
+      for (size_t i = 0; i < n; ++i) h = (h ^ b[i]) * 1099511628211ull;
+    };
+    const double d[] = {p.dx, p.dy, p.dz, p.dt, p.npower, p.k_max, p.alpha_max, p.rcoef, p.vpml,
+                        p.f0, p.t0, p.factor, p.src_w[0], p.src_w[1], p.src_w[2], p.angle_force};
+    const int32_t n[] = {p.stf, p.src_kind, p.src_i, p.src_j, p.src_k};
+    mix(d, sizeof d);
+    mix(n, sizeof n);
+    if (!rec.empty()) mix(rec.data(), rec.size() * sizeof(int32_t));
+    return h;
+  }
 
   int64_t checkpoint_bytes() const override {
     if (shots_.size() != 1) return -1;
@@ -924,7 +944,7 @@ class Engine final : public EngineBase {
     const Shot<T> &s = *shots_[0];
     CheckpointHeader h{};
     std::memcpy(h.magic, "ELA3DCK1", 8);
-    h.version = 1;
+    h.version = 2;
     h.precision = sizeof(T) == 8 ? ELA3D_FP64 : ELA3D_FP32;
     h.nx = s.p.nx; h.ny = s.p.ny; h.nz = s.p.nz;
     h.npml = s.p.npml; h.nstep = s.p.nstep; h.nrec = s.p.nrec; h.sampgat = s.p.sampgat;
@@ -932,6 +952,7 @@ class Engine final : public EngineBase {
     h.step = tick_ - s.d.tick0;
     h.pool_bytes = (int64_t)s.pool_bytes;
     h.e_ref = s.e_ref;
+    h.params_hash = params_hash(s.p, s.rec);
     return h;
   }
 
@@ -955,10 +976,10 @@ class Engine final : public EngineBase {
     if (std::memcmp(h.magic, mine.magic, 8) != 0 || h.version != mine.version) BAD("not an ela3d checkpoint");
     if (h.precision != mine.precision || h.nx != mine.nx || h.ny != mine.ny || h.nz != mine.nz ||
         h.npml != mine.npml || h.nstep != mine.nstep || h.nrec != mine.nrec || h.sampgat != mine.sampgat ||
-        h.pml_mode != mine.pml_mode || h.pool_bytes != mine.pool_bytes)
+        h.pml_mode != mine.pml_mode || h.pool_bytes != mine.pool_bytes || h.params_hash != mine.params_hash)
       BAD("checkpoint was written by a plan with other parameters");
     if (bytes < (int64_t)sizeof h + h.pool_bytes) BAD("checkpoint buffer truncated");
-    if (h.step < 0) BAD("checkpoint step out of range");
+    if (h.step < 0 || h.step > h.nstep) BAD("checkpoint step out of range");
     Shot<T> &s = *shots_[0];
     CK(cudaStreamSynchronize(stream_));
     CK(cudaMemcpy(s.pool, static_cast<const char *>(buf) + sizeof h, s.pool_bytes, cudaMemcpyHostToDevice));

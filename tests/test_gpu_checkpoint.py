@@ -1,6 +1,7 @@
 """Checkpoint / resume: a plan restored from a checkpoint continues exactly
 as the saved plan would have (bit for bit), in a fresh plan of the same
-parameters; a checkpoint of other parameters is refused."""
+parameters; a checkpoint of other parameters (sizes, time step, C-PML
+coefficients, source, receivers) is refused."""
 import numpy as np
 import pytest
 
@@ -48,14 +49,20 @@ def test_resume_from_checkpoint_is_bit_identical(built, precision):
             assert np.array_equal(x, y)
 
 
-def test_checkpoint_of_other_parameters_is_refused(built):
+@pytest.mark.parametrize("other", [{"npml": 6}, {"dt": 9e-4}, {"rcoef": 1e-4}, {"src": (16, 15, 12)},
+                                   {"f0": 24.0}, {"rec": np.array([[5, 6, 7], [20, 22, 9], [30, 3, 21]], np.int32)}],
+                         ids=["npml", "dt", "rcoef", "source", "f0", "receivers"])
+def test_checkpoint_of_other_parameters_is_refused(built, other):
+    """Sizes, time step, C-PML coefficients, source and receivers must all
+    match: the restoring plan recomputes its profiles and source table from
+    its own parameters, so any difference would change the continuation."""
     from ela3d_gb300 import Ela3dError, Plan
 
     p, cp, cs, rho = case()
     with Plan(p, cp, cs, rho) as a:
         a.run(3)
         ck = a.checkpoint()
-    q, cq, sq, rq = case(npml=6)
+    q, cq, sq, rq = case(**other)
     with Plan(q, cq, sq, rq) as b:
         with pytest.raises(Ela3dError) as e:
             b.restore(ck)
