@@ -63,7 +63,8 @@ struct ela3d_server {
   ela3d_server_config cfg{};
   int device = 0;
   std::mutex mu;
-  std::condition_variable cv_work, cv_done;
+  std::condition_variable cv_work, cv_done, cv_idle;
+  int waiters = 0;          // threads inside ela3d_server_wait
   std::deque<uint64_t> queue;
   std::map<uint64_t, std::unique_ptr<Request>> reqs;
   std::vector<uint64_t> running;
@@ -372,6 +373,14 @@ ela3d_status ela3d_server_read(ela3d_server *s, uint64_t ticket, int32_t first, 
 ela3d_status ela3d_server_wait(ela3d_server *s, uint64_t ticket, int32_t timeout_ms) {
   if (!s) return ELA3D_ERR_INVALID_ARG;
   std::unique_lock<std::mutex> lk(s->mu);
+  // counted, so that ela3d_server_destroy can let every waiter leave first
+  struct Count {
+    ela3d_server *s;
+    explicit Count(ela3d_server *q) : s(q) { ++s->waiters; }
+    ~Count() {
+      if (--s->waiters == 0) s->cv_idle.notify_all();
+    }
+  } count(s);
   auto done = [&] {
     auto it = s->reqs.find(ticket);
     return it == s->reqs.end() || it->second->state >= RQ_DONE;
@@ -444,6 +453,15 @@ ela3d_status ela3d_server_destroy(ela3d_server *s) {
     s->cv_work.notify_all();
   }
   if (s->worker.joinable()) s->worker.join();
+  {
+    // unfinished requests end as cancelled; threads waiting on them return
+    // ELA3D_ERR_CANCELLED before the server's memory goes away
+    std::unique_lock<std::mutex> lk(s->mu);
+    for (auto &kv : s->reqs)
+      if (kv.second->state < RQ_DONE) s->finish(*kv.second, RQ_CANCELLED, ELA3D_ERR_CANCELLED);
+    s->cv_done.notify_all();
+    s->cv_idle.wait(lk, [&] { return s->waiters == 0; });
+  }
   delete s;
   return ELA3D_OK;
 }

@@ -368,7 +368,10 @@ ela3d_status ela3d_server_cancel(ela3d_server *s, uint64_t ticket);
 /* Forgets a finished request (frees its host results). */
 ela3d_status ela3d_server_release(ela3d_server *s, uint64_t ticket);
 ela3d_status ela3d_server_stats_get(ela3d_server *s, ela3d_server_stats *out);
-/* Stops the worker; running requests are abandoned. */
+/* Stops the worker at the end of its current round; queued and running
+ * requests end as cancelled, and threads blocked in ela3d_server_wait return
+ * ELA3D_ERR_CANCELLED before this call returns.  No call may pass the server
+ * after that. */
 ela3d_status ela3d_server_destroy(ela3d_server *s);
 
 /* ---- host-side planning (no GPU needed) ---------------------------------- */

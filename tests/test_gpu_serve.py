@@ -168,3 +168,34 @@ def test_fp64_requests_equal_alone(built):
         for q, t in enumerate(tickets):
             srv.wait(t)
             assert np.array_equal(srv.read(t), want[q]), q
+
+
+def test_destroy_releases_waiting_clients(built):
+    """Destroying the server while client threads wait on unfinished requests
+    (one running, one queued behind a one-slot limit) ends those requests as
+    cancelled: every waiter returns ELA3D_ERR_CANCELLED, none is left
+    blocked on a server that no longer exists."""
+    from ela3d_gb300 import Ela3dError, Server
+
+    reqs = [request(s) for s in (40, 41)]
+    reqs = [(r[0].with_(nstep=50_000),) + tuple(r[1:]) for r in reqs]   # seconds of work each
+    srv = Server(steps_per_round=10, max_active=1)
+    tickets = [srv.submit(*r) for r in reqs]
+    got = {}
+
+    def client(q, t):
+        try:
+            srv.wait(t)
+            got[q] = 0
+        except Ela3dError as e:
+            got[q] = e.status
+
+    threads = [threading.Thread(target=client, args=(q, t)) for q, t in enumerate(tickets)]
+    for th in threads:
+        th.start()
+    time.sleep(0.3)
+    srv.close()
+    for th in threads:
+        th.join(timeout=30)
+        assert not th.is_alive()
+    assert got == {0: 8, 1: 8}   # ELA3D_ERR_CANCELLED
