@@ -139,7 +139,9 @@ ela3d_status ela3d_plan_create(const ela3d_params *p, const float *cp, const flo
                                const float *rho, ela3d_plan **out);
 /* Advances nsteps time steps (the it loop, simpelmodel.cpp:376-726) and
  * waits for completion; resumable.  Returns ELA3D_ERR_UNSTABLE when the
- * energy monitor trips, ELA3D_ERR_TIMEOUT when a kernel gave up a wait. */
+ * energy monitor trips, ELA3D_ERR_TIMEOUT when a kernel gave up a wait.
+ * Steps past nstep keep propagating the wavefield with no source and no
+ * recording (nstep sizes the source table and the seismogram buffers). */
 ela3d_status ela3d_run(ela3d_plan *plan, int32_t nsteps);
 /* ela3d_run bracketed by CUDA events on the plan's stream; *ms receives the
  * device time of the nsteps steps. */

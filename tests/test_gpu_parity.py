@@ -153,3 +153,29 @@ def test_energy_positive_and_decays(built):
         e2 = plan.energy()
     assert np.isfinite(e1) and e1 > 0
     assert e2 < e1
+
+
+def test_steps_past_nstep_propagate_without_source_or_recording(built):
+    """Past nstep the wavefield keeps moving with no source and no recording:
+    the seismograms and source trace stay those of the first nstep steps, and
+    a checkpoint taken there resumes as usual."""
+    from ela3d_gb300 import Plan
+
+    p, cp, cs, rho = small_case(nstep=60)
+    with Plan(p, cp, cs, rho) as plan:
+        plan.run(60)
+        s60, t60 = plan.seismograms(), plan.source_trace()
+        f60 = plan.field(2)
+        plan.run(25)
+        assert plan.info().step == 85
+        assert np.array_equal(plan.seismograms(), s60)
+        assert np.array_equal(plan.source_trace(), t60)
+        assert not np.array_equal(plan.field(2), f60)
+        ck = plan.checkpoint()
+        plan.run(10)
+        want = plan.field(2)
+    with Plan(p, cp, cs, rho) as again:
+        again.restore(ck)
+        assert again.info().step == 85
+        again.run(10)
+        assert np.array_equal(again.field(2), want)
