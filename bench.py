@@ -328,6 +328,9 @@ def run_ours(args, rank, world, local):
         v = E.variants()[best.variant]
         tune_info = {"source": "ela3d_autotune", "candidates": cand, "tile": [v.tile_x, v.tile_y],
                      "stages": v.stages, "schedule": best.schedule, "chunk": best.chunk, "prefetch": best.prefetch}
+    if args.prefetch >= 0:   # an explicit memory-variable prefetch mode (profiling comparisons)
+        tune["prefetch"] = args.prefetch
+        tune_info["prefetch"] = args.prefetch
     clocks = ClockSampler(local)
     plan = E.Plan(p, cp, cs, rho, **tune)
     plan.run(args.warmup)
@@ -615,6 +618,9 @@ def main():
                     help="skip the FP64 re-run of the end-to-end shot (accuracy of every seismogram and field)")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched and uneven workloads")
     ap.add_argument("--no-autotune", action="store_true", help="use the built-in kernel choice")
+    ap.add_argument("--prefetch", type=int, default=-1,
+                    help="C-PML memory-variable prefetch mode of the single-shot plan (ela3d_tuning.prefetch: "
+                         "0 none, 2 x slab into L1, 6 also y/z slabs into L2); -1 = tuned or built-in")
     ap.add_argument("--batch-shots", type=int, default=64)
     ap.add_argument("--batch-steps", type=int, default=100)
     ap.add_argument("--batch-schedule", type=int, default=2)
