@@ -328,9 +328,11 @@ def run_ours(args, rank, world, local):
         v = E.variants()[best.variant]
         tune_info = {"source": "ela3d_autotune", "candidates": cand, "tile": [v.tile_x, v.tile_y],
                      "stages": v.stages, "schedule": best.schedule, "chunk": best.chunk, "prefetch": best.prefetch}
-    if args.prefetch >= 0:   # an explicit memory-variable prefetch mode (profiling comparisons)
-        tune["prefetch"] = args.prefetch
-        tune_info["prefetch"] = args.prefetch
+    # explicit tuning fields (profiling comparisons)
+    for key, val in (("prefetch", args.prefetch), ("schedule", args.schedule), ("chunk", args.chunk)):
+        if val >= 0:
+            tune[key] = val
+            tune_info[key] = val
     clocks = ClockSampler(local)
     plan = E.Plan(p, cp, cs, rho, **tune)
     plan.run(args.warmup)
@@ -621,6 +623,10 @@ def main():
     ap.add_argument("--prefetch", type=int, default=-1,
                     help="C-PML memory-variable prefetch mode of the single-shot plan (ela3d_tuning.prefetch: "
                          "0 none, 2 x slab into L1, 6 also y/z slabs into L2); -1 = tuned or built-in")
+    ap.add_argument("--schedule", type=int, default=-1,
+                    help="work schedule of the single-shot plan (0 contiguous shares, 1 z-chunks round-robin); "
+                         "-1 = tuned or built-in")
+    ap.add_argument("--chunk", type=int, default=-1, help="z-chunk planes for --schedule 1; -1 = tuned or built-in")
     ap.add_argument("--batch-shots", type=int, default=64)
     ap.add_argument("--batch-steps", type=int, default=100)
     ap.add_argument("--batch-schedule", type=int, default=2)
