@@ -329,7 +329,8 @@ def run_ours(args, rank, world, local):
         tune_info = {"source": "ela3d_autotune", "candidates": cand, "tile": [v.tile_x, v.tile_y],
                      "stages": v.stages, "schedule": best.schedule, "chunk": best.chunk, "prefetch": best.prefetch}
     # explicit tuning fields (profiling comparisons)
-    for key, val in (("prefetch", args.prefetch), ("schedule", args.schedule), ("chunk", args.chunk)):
+    for key, val in (("variant", args.variant), ("prefetch", args.prefetch), ("schedule", args.schedule),
+                     ("chunk", args.chunk)):
         if val >= 0:
             tune[key] = val
             tune_info[key] = val
@@ -623,6 +624,9 @@ def main():
     ap.add_argument("--prefetch", type=int, default=-1,
                     help="C-PML memory-variable prefetch mode of the single-shot plan (ela3d_tuning.prefetch: "
                          "0 none, 2 x slab into L1, 6 also y/z slabs into L2); -1 = tuned or built-in")
+    ap.add_argument("--variant", type=int, default=-1,
+                    help="kernel variant (tile shape, stages) of the single-shot plan, an index of "
+                         "ela3d_gb300.variants(); -1 = tuned or built-in")
     ap.add_argument("--schedule", type=int, default=-1,
                     help="work schedule of the single-shot plan (0 contiguous shares, 1 z-chunks round-robin); "
                          "-1 = tuned or built-in")
