@@ -118,6 +118,7 @@ ela3d_status ela3d_variant_get(int32_t index, ela3d_variant_info *out) {
   out->threads = v[index].threads;
   out->stress_smem = v[index].stress_smem;
   out->velocity_smem = v[index].vel_smem;
+  out->loads = v[index].loads;
   return ELA3D_OK;
 }
 

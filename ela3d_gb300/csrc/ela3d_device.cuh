@@ -42,6 +42,11 @@ constexpr unsigned long long kTestWaitLimitNs = 20000000ull;
 // (performance hints; results do not depend on them).
 enum : int { CTL_WITHHOLD_LOADS = 1, CTL_PF_X = 2, CTL_PF_YZ = 4 };
 
+// How a kernel's loading warp fills a stage: one lane issues TMA tiled loads
+// (LOAD_TMA, every production variant), or all 32 lanes copy 16-byte chunks
+// with cp.async (LOAD_CP_ASYNC, kept as the measured alternative).
+enum : int { LOAD_TMA = 0, LOAD_CP_ASYNC = 1 };
+
 // Which psi variable of an axis.  Stress half-step: S0..S2, velocity: V0..V2.
 //  x: S0 dvx_dx(half) S1 dvy_dx S2 dvz_dx | V0 dsxx_dx V1 dsxy_dx(half) V2 dsxz_dx(half)
 //  y: S0 dvy_dy S1 dvx_dy(half) S2 dvz_dy(half) | V0 dsxy_dy V1 dsyy_dy(half) V2 dsyz_dy
@@ -156,6 +161,22 @@ __device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, i
       "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
       : "memory");
 }
+
+// 16-byte asynchronous copy global -> shared through L2 (cp.async.cg);
+// the first src_bytes (0..16) are read, the rest of the 16 are zero-filled.
+// Both addresses 16-byte aligned.
+__device__ __forceinline__ void cp_async_16(void *dst, const void *src, uint32_t src_bytes) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(smem_u32(dst)), "l"(src), "r"(src_bytes)
+               : "memory");
+}
+
+// Arrive on bar once every cp.async this thread issued before has landed
+// (the barrier's expected count includes this arrival).
+__device__ __forceinline__ void cp_async_arrive_noinc(uint64_t *bar) {
+  asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
 __device__ __forceinline__ void prefetch_tensormap(const CUtensorMap *map) {
   asm volatile("prefetch.tensormap [%0];" ::"l"(reinterpret_cast<uint64_t>(map)) : "memory");

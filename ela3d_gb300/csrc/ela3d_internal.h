@@ -16,6 +16,7 @@ struct Variant {
   int threads;          // threads per block
   int stress_smem, vel_smem;  // dynamic shared memory bytes
   int halo;             // x halo (elements) of the wide boxes
+  int loads;            // LOAD_TMA or LOAD_CP_ASYNC (how stages are filled)
   const void *stress;   // __global__ entry points
   const void *velocity;
 };

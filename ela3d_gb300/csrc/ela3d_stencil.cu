@@ -7,7 +7,7 @@
 
 namespace ela3d {
 
-template <typename T, int TX, int TY, int NS, int CPT = Vec<T>::N, int MB = 0>
+template <typename T, int TX, int TY, int NS, int CPT = Vec<T>::N, int MB = 0, int LOAD = LOAD_TMA>
 static Variant make_variant() {
   using G = Geo<T, TX, TY, NS, CPT, MB>;
   Variant v;
@@ -19,8 +19,9 @@ static Variant make_variant() {
   v.stress_smem = G::S_SMEM;
   v.vel_smem = G::V_SMEM;
   v.halo = G::H;
-  v.stress = reinterpret_cast<const void *>(&stress_kernel<T, TX, TY, NS, CPT, MB>);
-  v.velocity = reinterpret_cast<const void *>(&velocity_kernel<T, TX, TY, NS, CPT, MB>);
+  v.loads = LOAD;
+  v.stress = reinterpret_cast<const void *>(&stress_kernel<T, TX, TY, NS, CPT, MB, LOAD>);
+  v.velocity = reinterpret_cast<const void *>(&velocity_kernel<T, TX, TY, NS, CPT, MB, LOAD>);
   return v;
 }
 
@@ -31,6 +32,9 @@ static const Variant kVariants[] = {
     make_variant<float, 64, 14, 4>(),
     make_variant<float, 128, 3, 4>(),
     make_variant<float, 64, 6, 4>(),
+    // the 128x7 tile with its stages filled by cp.async instead of TMA (the
+    // measured alternative to the tensor-memory-accelerator loads)
+    make_variant<float, 128, 7, 4, 4, 0, LOAD_CP_ASYNC>(),
     // FP64 (the accuracy build; its rate on GB300 makes it compute-bound):
     // one cell per thread keeps it free of register spills
     make_variant<double, 32, 7, 4, 1>(),

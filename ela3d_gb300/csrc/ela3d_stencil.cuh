@@ -158,13 +158,38 @@ struct PsiPrefetch {
   }
 };
 
+// cp.async counterpart of one TMA box load: the BW x BH box of plane k of
+// `base` with origin (x, y), stored densely row by row like the TMA box;
+// cells outside [0, nx) x [0, ny) x [0, nz) read as zeros.  Each lane copies
+// every 32nd 16-byte chunk.
+template <typename T, int BW, int BH>
+__device__ __forceinline__ void copy_box_async(unsigned char *dst, const T *base, const ShotDesc<T> &sd, int x, int y,
+                                               int k, int lane) {
+  constexpr int E = 16 / (int)sizeof(T);  // elements per chunk
+  constexpr int CPR = BW / E, N = CPR * BH;
+  static_assert(BW % E == 0, "box rows are whole chunks");
+  const bool kin = k >= 0 && k < sd.nz;
+  for (int c = lane; c < N; c += 32) {
+    const int r = c / CPR, xx = x + (c - r * CPR) * E, yy = y + r;
+    uint32_t bytes = 0;
+    const T *src = base;
+    if (kin && yy >= 0 && yy < sd.ny && xx >= 0 && xx < sd.nx) {
+      bytes = (uint32_t)(min(E, sd.nx - xx) * (int)sizeof(T));
+      src = base + ((long long)k * sd.ny + yy) * sd.px + xx;
+    }
+    cp_async_16(dst + (size_t)c * 16, src, bytes);
+  }
+}
+
 // Producer warp: walks the block's items and issues every plane's loads
 // (lane 0) and the plane's memory-variable prefetches (all lanes).  Load n
 // goes to stage n % NS; before reusing a stage lane 0 waits for the
 // consumers' release of load n - NS on that stage's empty barrier.  Item i
 // contributes planes k0 .. k1 (k1 is the look-ahead plane, possibly nz,
 // which the TMA fills with zeros).
-template <int NS, typename Issue, typename Prefetch>
+// With ASYNC every lane copies a share of each plane's boxes (cp.async)
+// instead of lane 0 issuing TMA loads.
+template <int NS, bool ASYNC, typename Issue, typename Prefetch>
 __device__ __forceinline__ void produce(const Item *__restrict__ items, int2 range, uint64_t *full, uint64_t *empty,
                                         Issue issue, Prefetch &prefetch, unsigned *__restrict__ err, int ctl,
                                         int lane) {
@@ -182,10 +207,11 @@ __device__ __forceinline__ void produce(const Item *__restrict__ items, int2 ran
         ok = false;
         break;
       }
-      if (lane == 0) issue(it, k, slot, &full[slot]);
+      if (ASYNC || lane == 0) issue(it, k, slot, &full[slot], lane);
       prefetch.plane(k);
     }
   }
+  if (ASYNC) cp_async_wait_all();
   if (lane != 0) return;
   if (!ok) atomicOr(err, DEV_ERR_TIMEOUT);
   // the block must not exit with copies in flight
@@ -196,7 +222,7 @@ __device__ __forceinline__ void produce(const Item *__restrict__ items, int2 ran
 // ----------------------------------------------------------- stress ----
 // (tick and dtick are unused by the stress half-step; the parameter list is
 // shared with the velocity kernel so both launch from one argument array)
-template <typename T, int TX, int TY, int NS, int CPT, int MB>
+template <typename T, int TX, int TY, int NS, int CPT, int MB, int LOAD>
 __global__ void __launch_bounds__(Geo<T, TX, TY, NS, CPT, MB>::THREADS, Geo<T, TX, TY, NS, CPT, MB>::MINB)
     stress_kernel(const ShotDesc<T> *__restrict__ shots, const ShotMaps *__restrict__ maps,
                   const Item *__restrict__ items, const int2 *__restrict__ ranges, int tick,
@@ -213,7 +239,7 @@ __global__ void __launch_bounds__(Geo<T, TX, TY, NS, CPT, MB>::THREADS, Geo<T, T
 
   if (tid == 0) {
     for (int s = 0; s < NS; ++s) {
-      mbar_init(&full[s], 1);
+      mbar_init(&full[s], LOAD == LOAD_TMA ? 1 : 32);  // TMA: one arrive + bytes; else one per lane
       mbar_init(&empty[s], G::NCW);
     }
     fence_mbar_init();
@@ -222,10 +248,23 @@ __global__ void __launch_bounds__(Geo<T, TX, TY, NS, CPT, MB>::THREADS, Geo<T, T
 
   if (tid >= G::NT) {  // producer warp
     {
-      auto issue = [&](const Item &it, int k, int slot, uint64_t *bar) {
+      auto issue = [&](const Item &it, int k, int slot, uint64_t *bar, int lane) {
         const int txs = tiles_x_of(shots[it.shot], TX);
         const int x0 = (it.tile % txs) * TX, y0 = (it.tile / txs) * TY;
         unsigned char *st = smem + slot * G::S_STAGE;
+        if constexpr (LOAD == LOAD_CP_ASYNC) {
+          const ShotDesc<T> &sd = shots[it.shot];
+          copy_box_async<T, TX + H, TY + 1>(st + G::S_VX, sd.f[0], sd, x0, y0, k, lane);
+          copy_box_async<T, TX + H, TY + 1>(st + G::S_VY, sd.f[1], sd, x0 - H, y0 - 1, k, lane);
+          copy_box_async<T, TX + H, TY + 1>(st + G::S_VZ, sd.f[2], sd, x0 - H, y0, k, lane);
+          copy_box_async<T, TX + H, TY + 1>(st + G::S_CS, sd.cs, sd, x0 - H, y0, k, lane);
+          copy_box_async<T, TX + H, TY + 1>(st + G::S_RHO, sd.rho, sd, x0 - H, y0, k, lane);
+          copy_box_async<T, TX, TY>(st + G::S_CP, sd.cp, sd, x0, y0, k, lane);
+#pragma unroll
+          for (int c = 0; c < 6; ++c) copy_box_async<T, TX, TY>(st + G::S_SIG + c * G::SC, sd.f[3 + c], sd, x0, y0, k, lane);
+          cp_async_arrive_noinc(bar);
+          return;
+        }
         const CUtensorMap *m = maps[it.shot].stress;
         mbar_arrive_expect_tx(bar, G::S_TX);
         tma_load_3d(st + G::S_VX, &m[0], x0, y0, k, bar);
@@ -248,7 +287,7 @@ __global__ void __launch_bounds__(Geo<T, TX, TY, NS, CPT, MB>::THREADS, Geo<T, T
         }
         __device__ __forceinline__ void plane(int k) const { pf.plane(k); }
       } prefetch{{}, shots, tid - G::NT, ctl};
-      produce<NS>(items, range, full, empty, issue, prefetch, err, ctl, tid - G::NT);
+      produce<NS, LOAD == LOAD_CP_ASYNC>(items, range, full, empty, issue, prefetch, err, ctl, tid - G::NT);
     }
     return;
   }
@@ -549,7 +588,7 @@ __global__ void __launch_bounds__(Geo<T, TX, TY, NS, CPT, MB>::THREADS, Geo<T, T
 }
 
 // --------------------------------------------------------- velocity ----
-template <typename T, int TX, int TY, int NS, int CPT, int MB>
+template <typename T, int TX, int TY, int NS, int CPT, int MB, int LOAD>
 __global__ void __launch_bounds__(Geo<T, TX, TY, NS, CPT, MB>::THREADS, Geo<T, TX, TY, NS, CPT, MB>::MINB)
     velocity_kernel(const ShotDesc<T> *__restrict__ shots, const ShotMaps *__restrict__ maps,
                     const Item *__restrict__ items, const int2 *__restrict__ ranges, int tick,
@@ -566,7 +605,7 @@ __global__ void __launch_bounds__(Geo<T, TX, TY, NS, CPT, MB>::THREADS, Geo<T, T
 
   if (tid == 0) {
     for (int s = 0; s < NS; ++s) {
-      mbar_init(&full[s], 1);
+      mbar_init(&full[s], LOAD == LOAD_TMA ? 1 : 32);  // TMA: one arrive + bytes; else one per lane
       mbar_init(&empty[s], G::NCW);
     }
     fence_mbar_init();
@@ -575,10 +614,24 @@ __global__ void __launch_bounds__(Geo<T, TX, TY, NS, CPT, MB>::THREADS, Geo<T, T
 
   if (tid >= G::NT) {  // producer warp
     {
-      auto issue = [&](const Item &it, int k, int slot, uint64_t *bar) {
+      auto issue = [&](const Item &it, int k, int slot, uint64_t *bar, int lane) {
         const int txs = tiles_x_of(shots[it.shot], TX);
         const int x0 = (it.tile % txs) * TX, y0 = (it.tile / txs) * TY;
         unsigned char *st = smem + slot * G::V_STAGE;
+        if constexpr (LOAD == LOAD_CP_ASYNC) {
+          const ShotDesc<T> &sd = shots[it.shot];
+          copy_box_async<T, TX + H, TY>(st + G::V_SXX, sd.f[3], sd, x0 - H, y0, k, lane);
+          copy_box_async<T, TX, TY + 1>(st + G::V_SYY, sd.f[4], sd, x0, y0, k, lane);
+          copy_box_async<T, TX, TY>(st + G::V_SZZ, sd.f[5], sd, x0, y0, k, lane);
+          copy_box_async<T, TX + H, TY + 1>(st + G::V_SXY, sd.f[6], sd, x0, y0 - 1, k, lane);
+          copy_box_async<T, TX + H, TY>(st + G::V_SXZ, sd.f[7], sd, x0, y0, k, lane);
+          copy_box_async<T, TX, TY + 1>(st + G::V_SYZ, sd.f[8], sd, x0, y0 - 1, k, lane);
+          copy_box_async<T, TX + H, TY + 1>(st + G::V_RHO, sd.rho, sd, x0 - H, y0, k, lane);
+#pragma unroll
+          for (int c = 0; c < 3; ++c) copy_box_async<T, TX, TY>(st + G::V_V + c * G::SC, sd.f[c], sd, x0, y0, k, lane);
+          cp_async_arrive_noinc(bar);
+          return;
+        }
         const CUtensorMap *m = maps[it.shot].vel;
         mbar_arrive_expect_tx(bar, G::V_TX);
         tma_load_3d(st + G::V_SXX, &m[0], x0 - H, y0, k, bar);
@@ -602,7 +655,7 @@ __global__ void __launch_bounds__(Geo<T, TX, TY, NS, CPT, MB>::THREADS, Geo<T, T
         }
         __device__ __forceinline__ void plane(int k) const { pf.plane(k); }
       } prefetch{{}, shots, tid - G::NT, ctl};
-      produce<NS>(items, range, full, empty, issue, prefetch, err, ctl, tid - G::NT);
+      produce<NS, LOAD == LOAD_CP_ASYNC>(items, range, full, empty, issue, prefetch, err, ctl, tid - G::NT);
     }
     return;
   }

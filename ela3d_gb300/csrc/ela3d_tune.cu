@@ -129,7 +129,8 @@ ela3d_status autotune(const std::vector<ela3d_params> &ps, const std::vector<con
   double best_t = 1e300;
   TuneChoice bc{-1, 0, 0, 0};
   for (int v = 0; v < nv; ++v) {
-    if (vs[v].fp64 != fp64) continue;
+    // (the cp.async-filled variant is a measured alternative, 5-6x slower)
+    if (vs[v].fp64 != fp64 || vs[v].loads != LOAD_TMA) continue;
     // one engine per variant (the tensor maps depend on the tile); the
     // schedules and prefetch modes are switched in place
     ela3d_status st;

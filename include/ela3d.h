@@ -224,6 +224,9 @@ ela3d_status ela3d_plan_check_guards(ela3d_plan *plan);
 typedef struct ela3d_variant_info {
     int32_t fp64, tile_x, tile_y, stages, threads;
     int32_t stress_smem, velocity_smem;
+    int32_t loads;   /* 0: stages filled by TMA tiled loads; 1: by cp.async
+                        copies of the whole loading warp (a measured
+                        alternative, not a default) */
 } ela3d_variant_info;
 
 /* Work schedule: kind 0 = equal contiguous share of (tile, plane) units per

@@ -1,18 +1,32 @@
 """Padding poison: NaN written into every padding column (x >= nx of the
 padded rows) of the fields and C-PML memory variables never reaches a grid
 cell -- the tensor maps end at nx, so the stencils' loads fill zeros there
--- and the results are bit-identical to an unpoisoned run."""
+(the cp.async copies zero-fill from nx on as well) -- and the results are
+bit-identical to an unpoisoned run."""
 import numpy as np
 import pytest
 
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("nx,variant", [(37, 0), (45, 3), (29, 6)])
-def test_nan_padding_never_reaches_the_grid(built, nx, variant):
+def pick(kind):
+    """Index of a compiled variant: the default FP32 tile, the 64-wide FP32
+    tile, the FP32 tile filled by cp.async instead of TMA, the first FP64."""
+    import ela3d_gb300 as E
+
+    for i, v in enumerate(E.variants()):
+        if ((kind == "fp32" and not v.fp64 and v.loads == 0) or (kind == "fp32_64" and not v.fp64 and v.tile_x == 64)
+                or (kind == "cp_async" and v.loads == 1) or (kind == "fp64" and v.fp64)):
+            return i
+    raise LookupError(kind)
+
+
+@pytest.mark.parametrize("nx,kind", [(37, "fp32"), (45, "fp32_64"), (41, "cp_async"), (29, "fp64")])
+def test_nan_padding_never_reaches_the_grid(built, nx, kind):
     import ela3d_gb300 as E
     from ela3d_gb300 import Plan, ShotParams, media
 
+    variant = pick(kind)
     ny, nz = 26, 22
     cp, cs, rho = media.anticline_layers(nx, ny, nz, depths=(5, 11, 17, 40), amp=2, sigma=6, seed=7)
     fp64 = E.variants()[variant].fp64
