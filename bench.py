@@ -475,6 +475,7 @@ def uneven_batch(args) -> dict:
     together vs the same instances one at a time (each alone on the GPU)."""
     import ela3d_gb300 as E
     from ela3d_gb300 import configs
+    from ela3d_gb300.metrics import bytes_per_cell
 
     inst = configs.uneven_batch(count=args.uneven_count)
     steps = args.uneven_steps
@@ -497,10 +498,16 @@ def uneven_batch(args) -> dict:
         ms = b.run_timed(steps)
     value = cells * steps / (ms / 1e3) / 1e9
     sizes = [p.cells for p, *_ in inst]
+    # algorithmic bytes of one step of every instance (each at its own PML share)
+    step_bytes = sum(p.cells * bytes_per_cell(p.nx, p.ny, p.nz, p.npml)["step"] for p, *_ in inst)
+    peak, _ = measured_peaks()
     return {"workload": f"uneven_batch: {len(inst)} grids, edges from multiples of 16 in [64, 320] (seed 1), "
                         f"{min(sizes) / 1e6:.2f}-{max(sizes) / 1e6:.1f} Mcells, random 3-6 layer domes, FP32",
             "metric": METRIC, "value": value, "steps_timed": steps,
             "single_shot_sequential_value": alone, "ratio_vs_single_shot": value / alone, "tuning": tune_info,
+            "bytes_per_cell_update": step_bytes / cells,
+            "frac_of_hbm": step_bytes * steps / (ms / 1e3) / 1e9 / peak,
+            "single_shot_frac_of_hbm": step_bytes * steps / alone_s / 1e9 / peak,
             "timing": "CUDA events; the same steps of every instance, batched vs one plan at a time"}
 
 
@@ -514,6 +521,7 @@ def serving(args) -> dict:
 
     import ela3d_gb300 as E
     from ela3d_gb300 import configs
+    from ela3d_gb300.metrics import bytes_per_cell
 
     reqs = [configs.serving_request(1000 + q, t_end=args.serve_t_end) for q in range(args.serve_count)]
     work = [p.cells * p.nstep for p, *_ in reqs]
@@ -578,6 +586,10 @@ def serving(args) -> dict:
                 "p50_latency_s": st["latency_p50_s"], "p99_latency_s": st["latency_p99_s"],
                 "max_latency_s": st["latency_max_s"], "rounds": st["rounds"]}
     sizes = [p.cells for p, *_ in reqs]
+    # algorithmic bytes of the whole stream (each request at its own PML share)
+    stream_bytes = sum(p.cells * p.nstep * bytes_per_cell(p.nx, p.ny, p.nz, p.npml)["step"] for p, *_ in reqs)
+    peak, _ = measured_peaks()
+    busy_s = total / (sat["gcells_per_s_busy"] * 1e9)
     check = fp64_check([(f"request {q}", *reqs[q], reqs[q][0].nstep, s) for q, s in served.items()])
     return {"workload": f"serving stream: {len(reqs)} requests (seeded lognormal edges in [64, 384], "
                         f"{min(sizes) / 1e6:.2f}-{max(sizes) / 1e6:.1f} Mcells, t_end {args.serve_t_end} s "
@@ -586,6 +598,9 @@ def serving(args) -> dict:
             "p99_latency_s": sat["p99_latency_s"],
             "single_shot_sequential_value": alone, "single_shot_sequential_wall_value": total / alone_wall / 1e9,
             "ratio_vs_single_shot": sat["gcells_per_s_wall"] / alone,
+            "bytes_per_cell_update": stream_bytes / total,
+            "frac_of_hbm_busy": stream_bytes / busy_s / 1e9 / peak,
+            "single_shot_frac_of_hbm": stream_bytes / alone_s / 1e9 / peak,
             "sweep": rows, "saturation_with_fill_target": fill_row, "steps_per_round": args.serve_round,
             "fp64_check": check,
             "timing": "wall clock from first submission to last completion (requests submitted from host "
