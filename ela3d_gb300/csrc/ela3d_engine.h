@@ -40,6 +40,9 @@ void slab_extent(const double *a_full, const double *a_half, int n, int *lo, int
 struct ShotShape {
   int nx, ny, nz;
   int id = -1;   // shot index written into the items (-1: position in the list)
+  // C-PML slab bounds (cells x < xl or x >= xr lie in the x slab, ...);
+  // only the schedule's cost estimate uses them (-1: no slabs)
+  int xl = -1, xr = -1, yl = -1, yr = -1, zl = -1, zr = -1;
 };
 void build_schedule(const std::vector<ShotShape> &shots, int tx, int ty, int kind, int chunk,
                     int max_blocks, std::vector<Item> *items, std::vector<int2> *ranges);
