@@ -21,8 +21,8 @@ struct ela3d_batch {
 };
 
 // A caller's tuning fields, checked before any device work: -1 (0 for the
-// chunk) selects the default; a variant must exist in this build and match
-// the shots' precision.
+// chunk) selects the default; a variant must be compiled into the library
+// and match the shots' precision.
 ela3d_status ela3d::validate_tuning(const ela3d_tuning *t, int32_t precision) {
   if (!t) return ELA3D_OK;
   int nv = 0;

@@ -79,8 +79,9 @@ std::string tune_key(const std::vector<ela3d_params> &ps) {
   return k.str();
 }
 
-// A cached choice is used only if this build can run it (a cache file may
-// come from a build with other variants); otherwise it counts as a miss.
+// A cached choice is used only if the library can run it (a cache file may
+// come from a library compiled with other variants); otherwise it counts as
+// a miss.
 bool tune_lookup(const std::vector<ela3d_params> &ps, TuneChoice *out) {
   std::lock_guard<std::mutex> g(g_mu);
   load_locked();

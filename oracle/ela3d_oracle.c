@@ -1,6 +1,6 @@
 /*
  * ela3d_oracle.c -- float32 and float64 instances of the CPU restatement.
- * TEST INFRASTRUCTURE ONLY (the checker, never the product path).
+ * TEST INFRASTRUCTURE ONLY (the oracle, never the product path).
  * Build: gcc -O2 -ffp-contract=off -shared -fPIC (see oracle/build.py).
  * The instances are named oracle_run_f32 / oracle_run_f64 and
  * oracle_profiles_f32 / oracle_profiles_f64 (FN() pastes the suffix).

@@ -1,7 +1,7 @@
 /*
  * ela3d_oracle.h -- CPU restatement of the reference's SEISMIC_CPML time loop.
  *
- * TEST INFRASTRUCTURE ONLY.  This is the checker: tests/, the smoke entry and
+ * TEST INFRASTRUCTURE ONLY.  This is the oracle: tests/, the smoke entry and
  * bench.py's cpu_baseline leg may call it; the product library never does.
  *
  * It restates, in plain C, the single-threaded float32 program
