@@ -51,9 +51,9 @@ with Plan(p, cp, cs, rho) as a:
 """
 
 
-def test_cache_entry_this_build_cannot_run_is_ignored(built, tmp_path):
-    """A tuning cache file written by another build (a variant index this
-    build lacks, a schedule kind it does not know) counts as a miss: the plan
+def test_cache_entry_the_library_cannot_run_is_ignored(built, tmp_path):
+    """A tuning cache file written by another library (a variant index this
+    one lacks, a schedule kind it does not know) counts as a miss: the plan
     is created with the built-in choice instead of failing."""
     import os
     import subprocess
