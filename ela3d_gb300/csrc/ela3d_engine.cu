@@ -311,6 +311,9 @@ class Engine final : public EngineBase {
     CK(cudaGetDevice(&device_));
     CK(cudaDeviceGetAttribute(&num_sms_, cudaDevAttrMultiProcessorCount, device_));
     CK(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
+    // shots joining a running engine are prepared on their own stream, so
+    // their uploads overlap the launches in flight
+    CK(cudaStreamCreateWithFlags(&setup_, cudaStreamNonBlocking));
     CK(cudaMalloc(&d_err_, sizeof(unsigned)));
     CK(cudaMemset(d_err_, 0, sizeof(unsigned)));
     CK(cudaMalloc(&d_energy_, sizeof(double)));
@@ -355,7 +358,7 @@ class Engine final : public EngineBase {
       float *stage = nullptr;
       bool keep = false;
       ~Undo() {
-        if (stage) cudaFree(stage);
+        if (stage) cudaFreeAsync(stage, e->setup_);
         if (!keep) e->release_shot(*s);
       }
     } undo{this, &s};
@@ -396,14 +399,14 @@ class Engine final : public EngineBase {
         std::vector<T> id(6 * (size_t)strides[ax]);
         for (int q = 0; q < 6; ++q)
           for (int i = 0; i < strides[ax]; ++i) id[(size_t)q * strides[ax] + i] = (q == PR_A || q == PR_AH) ? T(0) : T(1);
-        CK(cudaMemcpyAsync(s.prof + off[ax], id.data(), id.size() * sizeof(T), cudaMemcpyHostToDevice, stream_));
+        CK(cudaMemcpyAsync(s.prof + off[ax], id.data(), id.size() * sizeof(T), cudaMemcpyHostToDevice, setup_));
       } else {
-        CK(Fp<T>::profile(a, s.prof + off[ax], stream_));
+        CK(Fp<T>::profile(a, s.prof + off[ax], setup_));
       }
     }
     std::vector<T> hprof(6 * (size_t)(px + ny + nz));
-    CK(cudaMemcpyAsync(hprof.data(), s.prof, s.prof_bytes, cudaMemcpyDeviceToHost, stream_));
-    CK(cudaStreamSynchronize(stream_));
+    CK(cudaMemcpyAsync(hprof.data(), s.prof, s.prof_bytes, cudaMemcpyDeviceToHost, setup_));
+    CK(cudaStreamSynchronize(setup_));
     for (int ax = 0; ax < 3; ++ax) {
       std::vector<double> af(ns[ax]), ah(ns[ax]);
       for (int i = 0; i < ns[ax]; ++i) {
@@ -457,8 +460,8 @@ class Engine final : public EngineBase {
     const size_t o_trace = take(3 * (size_t)(p.nstep + 1) * sizeof(T), "the source trace");
     s.pool_bytes = o;
     CK(cudaMalloc(&s.pool, s.pool_bytes));
-    CK(cudaMemsetAsync(s.pool, 0, s.pool_bytes, stream_));
-    for (const auto &g : s.guards) CK(cudaMemsetAsync(s.pool + g.off, kGuardByte, g.bytes, stream_));
+    CK(cudaMemsetAsync(s.pool, 0, s.pool_bytes, setup_));
+    for (const auto &g : s.guards) CK(cudaMemsetAsync(s.pool + g.off, kGuardByte, g.bytes, setup_));
 
     ShotDesc<T> &d = s.d;
     d.nx = nx; d.ny = ny; d.nz = nz; d.px = px;
@@ -503,28 +506,28 @@ class Engine final : public EngineBase {
     // 3. model: generated on the device, or uploaded into the padded layout
     if (shared_model_of < 0 && spec) {
       T *dst[3] = {const_cast<T *>(d.cp), const_cast<T *>(d.cs), const_cast<T *>(d.rho)};
-      CK(Fp<T>::model(*spec, nx, ny, nz, px, dst[0], dst[1], dst[2], stream_));
+      CK(Fp<T>::model(*spec, nx, ny, nz, px, dst[0], dst[1], dst[2], setup_));
     } else if (shared_model_of < 0) {
       const float *src[3] = {cp, cs, rho};
       T *dst[3] = {const_cast<T *>(d.cp), const_cast<T *>(d.cs), const_cast<T *>(d.rho)};
       if (sizeof(T) == 4) {
         for (int c = 0; c < 3; ++c)
           CK(cudaMemcpy2DAsync(dst[c], px * sizeof(T), src[c], nx * sizeof(float), nx * sizeof(float),
-                               (size_t)ny * nz, cudaMemcpyHostToDevice, stream_));
+                               (size_t)ny * nz, cudaMemcpyHostToDevice, setup_));
       } else {
-        CK(cudaMalloc(&undo.stage, (size_t)nx * ny * nz * sizeof(float)));
+        CK(cudaMallocAsync(reinterpret_cast<void **>(&undo.stage), (size_t)nx * ny * nz * sizeof(float), setup_));
         for (int c = 0; c < 3; ++c) {
           CK(cudaMemcpyAsync(undo.stage, src[c], (size_t)nx * ny * nz * sizeof(float), cudaMemcpyHostToDevice,
-                             stream_));
-          CK(Fp<T>::pad(undo.stage, dst[c], nx, ny, nz, px, stream_));
+                             setup_));
+          CK(Fp<T>::pad(undo.stage, dst[c], nx, ny, nz, px, setup_));
         }
-        CK(cudaStreamSynchronize(stream_));
+        CK(cudaStreamSynchronize(setup_));
       }
     }
     // 4. source time function (FP64 on the device)
     if (p.nstep > 0) {
       StfArgs sa{p.nstep, p.stf, p.f0, p.t0, p.factor, p.dt};
-      CK(Fp<T>::stf(sa, const_cast<T *>(d.stf), stream_));
+      CK(Fp<T>::stf(sa, const_cast<T *>(d.stf), setup_));
     }
     // 5. receivers sorted by (k, j, i) with a per-plane index
     {
@@ -540,11 +543,11 @@ class Engine final : public EngineBase {
       for (size_t r = 0; r < nrec; ++r) rp[rs[r].z + 1]++;
       for (int k = 0; k < nz; ++k) rp[k + 1] += rp[k];
       CK(cudaMemcpyAsync(const_cast<int *>(d.rec_plane), rp.data(), rp.size() * sizeof(int), cudaMemcpyHostToDevice,
-                         stream_));
+                         setup_));
       if (nrec)
         CK(cudaMemcpyAsync(const_cast<int4 *>(d.rec_sorted), rs.data(), nrec * sizeof(int4), cudaMemcpyHostToDevice,
-                           stream_));
-      CK(cudaStreamSynchronize(stream_));
+                           setup_));
+      CK(cudaStreamSynchronize(setup_));
     }
     if (p.src_kind == ELA3D_SRC_EXPLOSIVE) any_explosive_ = true;
     undo.keep = true;   // the shot is owned by the engine from here on
@@ -552,14 +555,16 @@ class Engine final : public EngineBase {
     if (finalized_) {  // a shot joining a running engine
       Shot<T> &ns = *shots_.back();
       ns.key = next_key_++;
+      // (its descriptor and tensor maps reach the device at the next
+      // schedule rebuild, when no launch reads the tables any more)
       ela3d_status st2 = encode_shot_maps(ns);
-      if (st2 == ELA3D_OK) st2 = upload_tables();
       if (st2 != ELA3D_OK) {
         release_shot(ns);
         shots_.pop_back();
         return st2;
       }
       sched_valid_ = false;
+      tables_dirty_ = true;
     } else {
       shots_.back()->key = next_key_++;
     }
@@ -567,6 +572,10 @@ class Engine final : public EngineBase {
   }
 
   uint64_t last_key() const override { return shots_.empty() ? 0 : shots_.back()->key; }
+
+  // True once every launch enqueued so far has finished (or failed: the
+  // caller's sync reports that).
+  bool idle() const override { return cudaStreamQuery(stream_) != cudaErrorNotReady; }
 
   int index_of(uint64_t key) const {
     for (int q = 0; q < (int)shots_.size(); ++q)
@@ -839,6 +848,12 @@ class Engine final : public EngineBase {
       if (retire_ && (it < 1 || it > shots_[q]->p.nstep)) continue;
       shapes.push_back({d.nx, d.ny, d.nz, q, d.xl, d.xr, d.yl, d.yr, d.zl, d.zr});
       key.push_back(q);
+    }
+    if (tables_dirty_) {
+      CK(cudaStreamSynchronize(stream_));  // no launch reads the old tables any more
+      ela3d_status st = upload_tables();
+      if (st != ELA3D_OK) return st;
+      tables_dirty_ = false;
     }
     if (!sched_key_.empty() && key == sched_key_ && sched_valid_) return ELA3D_OK;
     sched_key_ = key;
@@ -1231,8 +1246,9 @@ class Engine final : public EngineBase {
     if (d_tick_) cudaFree(d_tick_);
     invalidate_graph();
     if (stream_) cudaStreamDestroy(stream_);
+    if (setup_) cudaStreamDestroy(setup_);
     d_desc_ = nullptr; d_maps_ = nullptr; d_items_ = nullptr; d_ranges_ = nullptr;
-    d_err_ = nullptr; d_energy_ = nullptr; d_tick_ = nullptr; stream_ = nullptr;
+    d_err_ = nullptr; d_energy_ = nullptr; d_tick_ = nullptr; stream_ = nullptr; setup_ = nullptr;
   }
 
   struct Ev { cudaEvent_t e0, e1, e2; };
@@ -1252,6 +1268,8 @@ class Engine final : public EngineBase {
   size_t items_cap_ = 0, ranges_cap_ = 0;
   std::vector<int> sched_key_;
   bool sched_valid_ = false, retire_ = false;
+  bool tables_dirty_ = false;  // a shot joined since the device tables were written
+  cudaStream_t setup_ = nullptr;
   int tick_ = 0;
   int inject_ = 0;   // steps left whose launches withhold their loads (test hook)
   int prefetch_ = kPrefetchDefault;  // memory-variable prefetch hints (x slab to L1, y/z slabs to L2)

@@ -99,6 +99,7 @@ class EngineBase {
   virtual void set_retire(bool on) = 0;
   // live composition (serving): shots may join after finalize and leave
   virtual uint64_t last_key() const = 0;  // key of the most recently added shot
+  virtual bool idle() const = 0;           // every enqueued launch has finished
   virtual ela3d_status remove_shot(uint64_t key) = 0;
   virtual int64_t footprint(const ela3d_params &p) const = 0;
   virtual int shot_steps(uint64_t key) const = 0;

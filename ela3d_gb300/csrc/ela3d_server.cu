@@ -3,17 +3,18 @@
 // per process.
 //
 // A worker thread owns one engine (the batched kernels).  Each round it
-//  1. admits queued requests in arrival order while their device footprint
-//     fits the budget, a slot is free and the running shots hold fewer cells
-//     than the fill target (a request larger than the whole budget is
-//     refused with ELA3D_ERR_BUSY);
-//  2. advances every running shot by up to `steps_per_round` time steps in
+//  1. enqueues up to `steps_per_round` time steps of every running shot in
 //     one launch pair per step (shots that reach their nstep inside the
 //     round stop there);
+//  2. while the device works, admits queued requests in arrival order while
+//     their device footprint fits the budget, a slot is free and the
+//     running shots hold fewer cells than the fill target (a request larger
+//     than the whole budget is refused with ELA3D_ERR_BUSY); their uploads
+//     run on the engine's setup stream, and they join at the next round;
 //  3. copies each running shot's new seismogram samples to its host buffer
 //     (clients read them while the shot runs);
 //  4. retires finished and cancelled shots, which frees their memory for
-//     the next round's admissions.
+//     later admissions.
 // Requests that arrive while others run join at the next round boundary,
 // so their work overlaps on the device with the shots already running.
 #include <algorithm>
@@ -98,95 +99,128 @@ struct ela3d_server {
     }
   }
 
-  void loop() {
-    cudaSetDevice(device);
-    std::unique_lock<std::mutex> lk(mu);
-    while (true) {
-      cv_work.wait(lk, [&] { return stop || !queue.empty() || !running.empty(); });
-      if (stop) break;
-      // admission, in arrival order
-      std::vector<Request *> admit;
-      double active_cells = 0.0;   // held by running and just-admitted shots
+  // The next request to admit, in arrival order, taken off the queue (with
+  // its device bytes booked), or null when the front request must wait for
+  // memory, a slot or the fill target.  Cancelled and oversize requests at
+  // the front are finished on the way.  Called with the lock held.
+  Request *take_admissible() {
+    while (!queue.empty()) {
+      Request &r = *reqs[queue.front()];
+      if (r.cancel) {
+        queue.pop_front();
+        finish(r, RQ_CANCELLED, ELA3D_ERR_CANCELLED);
+        cv_done.notify_all();
+        continue;
+      }
+      if (r.footprint > budget) {
+        queue.pop_front();
+        finish(r, RQ_FAILED, ELA3D_ERR_BUSY);
+        cv_done.notify_all();
+        continue;
+      }
+      double active_cells = 0.0;   // held by the running shots
       for (uint64_t t : running) {
         const ela3d_params &q = reqs[t]->p;
         active_cells += (double)q.nx * q.ny * q.nz;
       }
-      while (!queue.empty()) {
-        Request &r = *reqs[queue.front()];
-        if (r.cancel) {
-          queue.pop_front();
-          finish(r, RQ_CANCELLED, ELA3D_ERR_CANCELLED);
-          continue;
-        }
-        if (r.footprint > budget) {
-          queue.pop_front();
-          finish(r, RQ_FAILED, ELA3D_ERR_BUSY);
-          continue;
-        }
-        const bool slot = cfg.max_active <= 0 || (int)(running.size() + admit.size()) < cfg.max_active;
-        const bool fill = cfg.fill_cells <= 0 || active_cells < (double)cfg.fill_cells;
-        if (!slot || !fill || used + r.footprint > budget) break;
-        queue.pop_front();
-        used += r.footprint;
-        active_cells += (double)r.p.nx * r.p.ny * r.p.nz;
-        admit.push_back(&r);
-      }
+      const bool slot = cfg.max_active <= 0 || (int)running.size() < cfg.max_active;
+      const bool fill = cfg.fill_cells <= 0 || active_cells < (double)cfg.fill_cells;
+      if (!slot || !fill || used + r.footprint > budget) return nullptr;
+      queue.pop_front();
+      used += r.footprint;
+      return &r;
+    }
+    return nullptr;
+  }
+
+  void loop() {
+    cudaSetDevice(device);
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    cudaEventCreate(&ev0);
+    cudaEventCreate(&ev1);
+    std::unique_lock<std::mutex> lk(mu);
+    while (true) {
+      cv_work.wait(lk, [&] { return stop || !queue.empty() || !running.empty(); });
+      if (stop) break;
+      // cancellations of running shots take effect at this round boundary
       std::vector<Request *> cancelled;
       for (uint64_t t : running)
         if (reqs[t]->cancel) cancelled.push_back(reqs[t].get());
+      if (!cancelled.empty()) {
+        lk.unlock();
+        for (Request *r : cancelled) eng->remove_shot(r->key);
+        lk.lock();
+        for (Request *r : cancelled) {
+          used -= r->footprint;
+          running.erase(std::remove(running.begin(), running.end(), r->ticket), running.end());
+          finish(*r, RQ_CANCELLED, ELA3D_ERR_CANCELLED);
+        }
+        cv_done.notify_all();
+      }
+      // this round: the shots running now, up to the configured number of
+      // steps, no further than the longest remaining shot
+      std::vector<uint64_t> run_now = running;
+      int round = 0;
+      if (!run_now.empty()) {
+        int longest = 0;
+        for (uint64_t t : run_now) {
+          const Request &r = *reqs[t];
+          longest = std::max(longest, r.p.nstep - std::max(0, eng->shot_steps(r.key)));
+        }
+        round = std::max(1, std::min(std::max(1, cfg.steps_per_round), longest));
+      }
       lk.unlock();
 
-      // engine work happens without the lock (clients may submit/read)
-      std::vector<std::pair<Request *, ela3d_status>> admitted;
-      for (Request *r : admit) {
+      ela3d_status st = ELA3D_OK;
+      if (round > 0) {
+        cudaEventRecord(ev0, eng->stream());
+        st = eng->enqueue(round);
+        cudaEventRecord(ev1, eng->stream());
+      }
+      // admissions, in arrival order, while the device runs the round (a
+      // joining shot is prepared on its own stream and takes part from the
+      // next round on); once the round has finished, the rest wait for the
+      // next boundary.  With nothing running, the first admission starts
+      // the device and the others join while it works.
+      for (bool any = false;;) {
+        Request *r = nullptr;
+        {
+          std::lock_guard<std::mutex> g(mu);
+          r = take_admissible();
+        }
+        if (!r) break;
         ela3d_params p = r->p;
         p.rec = r->rec.data();
-        ela3d_status st = r->generated ? eng->add_shot(p, nullptr, nullptr, nullptr, -1, &r->spec)
-                                       : eng->add_shot(p, r->cp.data(), r->cs.data(), r->rho.data(), -1);
-        admitted.push_back({r, st});
-        if (st == ELA3D_OK) r->key = eng->last_key();
-      }
-      for (Request *r : cancelled) eng->remove_shot(r->key);
-
-      lk.lock();
-      for (auto &a : admitted) {
-        Request &r = *a.first;
-        if (a.second != ELA3D_OK) {
-          used -= r.footprint;
-          finish(r, RQ_FAILED, a.second);
-          continue;
+        const ela3d_status sa = r->generated ? eng->add_shot(p, nullptr, nullptr, nullptr, -1, &r->spec)
+                                             : eng->add_shot(p, r->cp.data(), r->cs.data(), r->rho.data(), -1);
+        {
+          std::lock_guard<std::mutex> g(mu);
+          if (sa != ELA3D_OK) {
+            used -= r->footprint;
+            finish(*r, RQ_FAILED, sa);
+          } else {
+            r->key = eng->last_key();
+            r->state = RQ_RUNNING;
+            r->t_admit = now_s();
+            r->cp.clear(); r->cp.shrink_to_fit();
+            r->cs.clear(); r->cs.shrink_to_fit();
+            r->rho.clear(); r->rho.shrink_to_fit();
+            running.push_back(r->ticket);
+            any = true;
+          }
+          cv_done.notify_all();
         }
-        r.state = RQ_RUNNING;
-        r.t_admit = now_s();
-        r.cp.clear(); r.cp.shrink_to_fit();
-        r.cs.clear(); r.cs.shrink_to_fit();
-        r.rho.clear(); r.rho.shrink_to_fit();
-        running.push_back(r.ticket);
+        if (round > 0 ? eng->idle() : any) break;
       }
-      for (Request *r : cancelled) {
-        used -= r->footprint;
-        running.erase(std::remove(running.begin(), running.end(), r->ticket), running.end());
-        finish(*r, RQ_CANCELLED, ELA3D_ERR_CANCELLED);
+      if (round == 0) {
+        lk.lock();
+        continue;
       }
-      cv_done.notify_all();
-      if (running.empty()) continue;
-      // steps of this round: up to the configured size, no further than the
-      // longest remaining shot
-      int round = std::max(1, cfg.steps_per_round);
-      int longest = 0;
-      for (uint64_t t : running) {
-        const Request &r = *reqs[t];
-        longest = std::max(longest, r.p.nstep - std::max(0, eng->shot_steps(r.key)));
-      }
-      round = std::max(1, std::min(round, longest));
-      std::vector<uint64_t> run_now = running;
-      lk.unlock();
 
-      const double t0 = now_s();
-      ela3d_status st = eng->enqueue(round);
       if (st == ELA3D_OK) st = eng->sync();
-      const double t1 = now_s();
-      // stream new samples
+      float round_ms = 0.0f;
+      if (st == ELA3D_OK) cudaEventElapsedTime(&round_ms, ev0, ev1);
+      // stream new samples of the shots that ran
       struct Chunk { Request *r; int from, to, steps; std::vector<float> data; ela3d_status st; };
       std::vector<Chunk> chunks;
       for (uint64_t t : run_now) {
@@ -207,7 +241,7 @@ struct ela3d_server {
       }
 
       lk.lock();
-      busy_s += t1 - t0;
+      busy_s += round_ms / 1e3;
       ++rounds;
       for (Chunk &c : chunks) {
         Request &r = *c.r;
@@ -227,6 +261,8 @@ struct ela3d_server {
       if (st != ELA3D_OK) fatal = st;
       cv_done.notify_all();
     }
+    cudaEventDestroy(ev0);
+    cudaEventDestroy(ev1);
   }
 };
 
