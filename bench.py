@@ -502,8 +502,12 @@ def uneven_batch(args) -> dict:
     with E.Batch(inst, **tune) as b:
         b.run(3)
         ms = b.run_timed(steps)
+        # two instances drawn by seed, as computed in the batch, against FP64
+        pick = sorted(np.random.default_rng(2).choice(len(inst), 2, replace=False).tolist())
+        seis = {q: b.seismograms(q) for q in pick}
     value = cells * steps / (ms / 1e3) / 1e9
     sizes = [p.cells for p, *_ in inst]
+    check = fp64_check([(f"instance {q}", *inst[q], 3 + steps, seis[q]) for q in pick])
     # algorithmic bytes of one step of every instance (each at its own PML share)
     step_bytes = sum(p.cells * bytes_per_cell(p.nx, p.ny, p.nz, p.npml)["step"] for p, *_ in inst)
     peak, _ = measured_peaks()
@@ -514,7 +518,7 @@ def uneven_batch(args) -> dict:
             "ratio_vs_single_shot": value / alone, "tuning": tune_info,
             "bytes_per_cell_update": step_bytes / cells,
             "frac_of_hbm": step_bytes * steps / (ms / 1e3) / 1e9 / peak,
-            "single_shot_frac_of_hbm": step_bytes * steps / alone_s / 1e9 / peak,
+            "single_shot_frac_of_hbm": step_bytes * steps / alone_s / 1e9 / peak, "fp64_check": check,
             "timing": "CUDA events; the same steps of every instance, batched vs one plan at a time (each "
                       "with the better of the built-in and the tuned kernel choice; default value: built-in only)"}
 
