@@ -25,6 +25,7 @@
 #include <map>
 #include <mutex>
 #include <new>
+#include <string>
 #include <thread>
 #include <vector>
 
@@ -51,6 +52,7 @@ struct Request {
   int64_t footprint = 0;
   int state = RQ_QUEUED;
   ela3d_status error = ELA3D_OK;
+  std::string message;             // the worker's error text for a failed request
   uint64_t key = 0;                // engine shot while running
   int nsamp = 0, samples_ready = 0;
   std::vector<float> seis;         // [nrec][3][nsamp]
@@ -83,6 +85,9 @@ struct ela3d_server {
   void finish(Request &r, int state, ela3d_status err) {
     r.state = state;
     r.error = err;
+    // (error texts are per thread: keep the worker's for the client)
+    if (state == RQ_FAILED) r.message = err == ELA3D_ERR_BUSY ? "request larger than the server's device budget"
+                                                                : std::string(last_error());
     r.t_done = now_s();
     r.cp.clear(); r.cp.shrink_to_fit();
     r.cs.clear(); r.cs.shrink_to_fit();
@@ -391,7 +396,9 @@ ela3d_status ela3d_server_poll(ela3d_server *s, uint64_t ticket, int32_t *state,
   if (it == s->reqs.end()) return ELA3D_ERR_NOT_FOUND;
   if (state) *state = it->second->state;
   if (samples_ready) *samples_ready = it->second->samples_ready;
-  return it->second->state == RQ_FAILED ? it->second->error : ELA3D_OK;
+  if (it->second->state != RQ_FAILED) return ELA3D_OK;
+  set_last_error(it->second->message);
+  return it->second->error;
 }
 
 ela3d_status ela3d_server_read(ela3d_server *s, uint64_t ticket, int32_t first, int32_t count, float *out) {
@@ -426,6 +433,7 @@ ela3d_status ela3d_server_wait(ela3d_server *s, uint64_t ticket, int32_t timeout
   auto it = s->reqs.find(ticket);
   if (it == s->reqs.end()) return ELA3D_ERR_NOT_FOUND;
   if (it->second->state == RQ_DONE) return ELA3D_OK;
+  if (it->second->state == RQ_FAILED) set_last_error(it->second->message);
   return it->second->error != ELA3D_OK ? it->second->error : ELA3D_ERR_CANCELLED;
 }
 

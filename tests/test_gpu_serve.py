@@ -84,6 +84,7 @@ def test_cancel_and_oversize_leave_others_identical(built):
         with pytest.raises(Ela3dError) as e:
             srv.wait(t_big)
         assert e.value.status == 7   # ELA3D_ERR_BUSY: larger than the whole budget
+        assert "budget" in str(e.value)   # the worker's reason reaches the client thread
         for q, t in enumerate(tickets):
             if q == 2:
                 with pytest.raises(Ela3dError):
