@@ -19,6 +19,9 @@ LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_build", "l
 # (name, restype, argtypes) of every entry point declared in include/ela3d.h
 _c = ctypes
 _P = _c.c_void_p
+# ela3d_request_callback: (ticket, status, user)
+REQUEST_CALLBACK = _c.CFUNCTYPE(None, _c.c_uint64, _c.c_int, _c.c_void_p)
+
 SIGNATURES = [
     ("ela3d_version", _c.c_char_p, []),
     ("ela3d_status_string", _c.c_char_p, [_c.c_int]),
@@ -68,6 +71,7 @@ SIGNATURES = [
     ("ela3d_server_wait", _c.c_int, [_P, _c.c_uint64, _c.c_int32]),
     ("ela3d_server_cancel", _c.c_int, [_P, _c.c_uint64]),
     ("ela3d_server_release", _c.c_int, [_P, _c.c_uint64]),
+    ("ela3d_server_on_done", _c.c_int, [_P, _c.c_uint64, REQUEST_CALLBACK, _c.c_void_p]),
     ("ela3d_server_stats_get", _c.c_int, [_P, _P]),
     ("ela3d_server_destroy", _c.c_int, [_P]),
     ("ela3d_autotune", _c.c_int, [_c.c_int32, _P, _P, _P, _P, _c.c_int32, _P, _c.POINTER(_c.c_double),
@@ -484,6 +488,7 @@ class Server:
         _check(lib.ela3d_server_create(ctypes.byref(cfg), ctypes.byref(h)), "ela3d_server_create")
         self._h = h
         self._params = {}
+        self._callbacks = {}
 
     def submit(self, params: ShotParams, cp, cs, rho) -> int:
         c, rec = params.to_c()
@@ -526,6 +531,13 @@ class Server:
 
     def cancel(self, ticket: int) -> None:
         _check(self._lib.ela3d_server_cancel(self._h, ticket), "ela3d_server_cancel")
+
+    def on_done(self, ticket: int, fn) -> None:
+        """fn(ticket, status) once the request ends (status 0: done); called
+        on the server's worker thread, or at once if it has already ended."""
+        cb = REQUEST_CALLBACK(lambda t, st, _user: fn(int(t), int(st)))
+        self._callbacks[ticket] = cb   # kept alive until the server is closed
+        _check(self._lib.ela3d_server_on_done(self._h, ticket, cb, None), "ela3d_server_on_done")
 
     def release(self, ticket: int) -> None:
         _check(self._lib.ela3d_server_release(self._h, ticket), "ela3d_server_release")

@@ -58,6 +58,15 @@ struct Request {
   std::vector<float> seis;         // [nrec][3][nsamp]
   double t_submit = 0, t_admit = 0, t_done = 0;
   bool cancel = false;
+  ela3d_request_callback on_done = nullptr;  // called once when the request ends
+  void *on_done_user = nullptr;
+};
+
+struct Callback {
+  ela3d_request_callback fn;
+  uint64_t ticket;
+  ela3d_status status;
+  void *user;
 };
 
 }  // namespace
@@ -81,6 +90,7 @@ struct ela3d_server {
   double cell_updates = 0, busy_s = 0, t_first = 0, t_last = 0;
   std::vector<double> latencies;
   ela3d_status fatal = ELA3D_OK;
+  std::vector<Callback> callbacks;   // due, to be called without the lock
 
   void finish(Request &r, int state, ela3d_status err) {
     r.state = state;
@@ -92,6 +102,10 @@ struct ela3d_server {
     r.cp.clear(); r.cp.shrink_to_fit();
     r.cs.clear(); r.cs.shrink_to_fit();
     r.rho.clear(); r.rho.shrink_to_fit();
+    if (r.on_done) {
+      callbacks.push_back({r.on_done, r.ticket, state == RQ_DONE ? ELA3D_OK : err, r.on_done_user});
+      r.on_done = nullptr;
+    }
     if (state == RQ_DONE) {
       ++n_completed;
       latencies.push_back(r.t_done - r.t_submit);
@@ -102,6 +116,17 @@ struct ela3d_server {
     } else {
       ++n_failed;
     }
+  }
+
+  // Calls the due completion callbacks; the lock must not be held (a
+  // callback may call back into the server).
+  void run_callbacks() {
+    std::vector<Callback> due;
+    {
+      std::lock_guard<std::mutex> g(mu);
+      due.swap(callbacks);
+    }
+    for (const Callback &c : due) c.fn(c.ticket, c.status, c.user);
   }
 
   // The next request to admit, in arrival order, taken off the queue (with
@@ -217,6 +242,7 @@ struct ela3d_server {
         }
         if (round > 0 ? eng->idle() : any) break;
       }
+      run_callbacks();
       if (round == 0) {
         lk.lock();
         continue;
@@ -265,6 +291,9 @@ struct ela3d_server {
       }
       if (st != ELA3D_OK) fatal = st;
       cv_done.notify_all();
+      lk.unlock();
+      run_callbacks();
+      lk.lock();
     }
     cudaEventDestroy(ev0);
     cudaEventDestroy(ev1);
@@ -447,6 +476,26 @@ ela3d_status ela3d_server_cancel(ela3d_server *s, uint64_t ticket) {
   return ELA3D_OK;
 }
 
+ela3d_status ela3d_server_on_done(ela3d_server *s, uint64_t ticket, ela3d_request_callback cb, void *user) {
+  if (!s || !cb) return ELA3D_ERR_INVALID_ARG;
+  Callback now{nullptr, ticket, ELA3D_OK, user};
+  {
+    std::lock_guard<std::mutex> g(s->mu);
+    auto it = s->reqs.find(ticket);
+    if (it == s->reqs.end()) return ELA3D_ERR_NOT_FOUND;
+    Request &r = *it->second;
+    if (r.state < RQ_DONE) {
+      r.on_done = cb;
+      r.on_done_user = user;
+      return ELA3D_OK;
+    }
+    now.fn = cb;   // already over: called right here, on this thread
+    now.status = r.state == RQ_DONE ? ELA3D_OK : (r.error != ELA3D_OK ? r.error : ELA3D_ERR_CANCELLED);
+  }
+  now.fn(now.ticket, now.status, now.user);
+  return ELA3D_OK;
+}
+
 ela3d_status ela3d_server_release(ela3d_server *s, uint64_t ticket) {
   if (!s) return ELA3D_ERR_INVALID_ARG;
   std::lock_guard<std::mutex> g(s->mu);
@@ -506,6 +555,7 @@ ela3d_status ela3d_server_destroy(ela3d_server *s) {
     s->cv_done.notify_all();
     s->cv_idle.wait(lk, [&] { return s->waiters == 0; });
   }
+  s->run_callbacks();
   delete s;
   return ELA3D_OK;
 }

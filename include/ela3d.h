@@ -370,6 +370,16 @@ ela3d_status ela3d_server_read(ela3d_server *s, uint64_t ticket, int32_t first, 
 ela3d_status ela3d_server_wait(ela3d_server *s, uint64_t ticket, int32_t timeout_ms);
 /* Stops a queued or running request at the next round boundary. */
 ela3d_status ela3d_server_cancel(ela3d_server *s, uint64_t ticket);
+/* Completion callback: called exactly once when the request ends, with
+ * ELA3D_OK (done), its error, or ELA3D_ERR_CANCELLED.  The server's worker
+ * thread calls it with no lock held, so it may call the other
+ * ela3d_server_* functions except ela3d_server_destroy; a request that has
+ * already ended gets its call at once, on the registering thread, and those
+ * ended by ela3d_server_destroy get theirs on the destroying thread before
+ * it returns.  One callback per request (a later registration replaces an
+ * earlier one). */
+typedef void (*ela3d_request_callback)(uint64_t ticket, ela3d_status status, void *user);
+ela3d_status ela3d_server_on_done(ela3d_server *s, uint64_t ticket, ela3d_request_callback cb, void *user);
 /* Forgets a finished request (frees its host results). */
 ela3d_status ela3d_server_release(ela3d_server *s, uint64_t ticket);
 ela3d_status ela3d_server_stats_get(ela3d_server *s, ela3d_server_stats *out);

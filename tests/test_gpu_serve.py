@@ -200,3 +200,47 @@ def test_destroy_releases_waiting_clients(built):
         th.join(timeout=30)
         assert not th.is_alive()
     assert got == {0: 8, 1: 8}   # ELA3D_ERR_CANCELLED
+
+
+def test_completion_callbacks_once_each_with_the_final_status(built):
+    """ela3d_server_on_done: every request's callback runs exactly once with
+    its final status -- done, cancelled while queued, cancelled while
+    running, refused as oversize, or cancelled by the server's destruction --
+    and a callback may read the results (it is called without the server's
+    lock).  One slot at a time makes every outcome deterministic."""
+    from ela3d_gb300 import Server
+
+    reqs = [request(s) for s in range(60, 64)]
+    want = [alone(*r) for r in reqs]
+    calls, seen = [], {}
+
+    def done(t, st):
+        calls.append((t, st))
+        if st == 0:
+            seen[t] = srv.read(t)
+
+    long_p = reqs[0][0].with_(nstep=50_000)                         # seconds of work
+    srv = Server(steps_per_round=20, variant=0, hbm_budget_bytes=256 << 20, max_active=1)
+    t_first = srv.submit(long_p, *reqs[0][1:])                      # holds the only slot
+    tickets = [srv.submit(*r) for r in reqs]                        # queued behind it
+    big_p = reqs[1][0].with_(nx=400, ny=400, nz=200, rec=np.zeros((0, 3), np.int32), src=(5, 5, 5))
+    m = np.ones(big_p.cells, np.float32)
+    t_big = srv.submit(big_p, m * 3000, m * 1700, m * 2000)         # larger than the budget
+    t_last = srv.submit(long_p, *reqs[0][1:])                       # still running at close
+    for t in [t_first, *tickets, t_big, t_last]:
+        srv.on_done(t, done)
+    srv.cancel(tickets[3])                                          # while queued
+    srv.cancel(t_first)                                             # while running
+    for t in tickets[:3]:
+        srv.wait(t)
+    late = []
+    srv.on_done(tickets[0], lambda t, st: late.append((t, st)))     # already over: called at once
+    assert late == [(tickets[0], 0)]
+    srv.close()
+    got = dict(calls)
+    assert len(calls) == len(got) == 7
+    assert [got[t] for t in tickets[:3]] == [0, 0, 0]
+    # ELA3D_ERR_CANCELLED (queued, running, at destruction), ELA3D_ERR_BUSY
+    assert (got[tickets[3]], got[t_first], got[t_last], got[t_big]) == (8, 8, 8, 7)
+    for q in range(3):
+        assert np.array_equal(seen[tickets[q]], want[q])
