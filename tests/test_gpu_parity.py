@@ -61,6 +61,10 @@ CASES = {
     "pml_covers_grid": {"shape": (16, 18, 20), "npml": 9, "nstep": 60},
     "no_pml": {"npml": 0},
     "explosive_far_corner": {"stf": 1, "src_kind": 1, "src": (0, 33, 45)},
+    # per-axis spacings (the reference hard-codes DELTAY = DELTAZ = DELTAX;
+    # the API takes three, and both restatements use each where it belongs)
+    "anisotropic_spacing_compat": {"dx": 10.0, "dy": 12.5, "dz": 8.0},
+    "anisotropic_spacing_clean": {"dx": 10.0, "dy": 12.5, "dz": 8.0, "pml_mode": 1},
 }
 
 
