@@ -183,3 +183,21 @@ def test_steps_past_nstep_propagate_without_source_or_recording(built):
         assert again.info().step == 85
         again.run(10)
         assert np.array_equal(again.field(2), want)
+
+
+@pytest.mark.parametrize("shape,npml", [((3, 3, 3), 0), ((3, 4, 5), 1), ((5, 3, 4), 1)])
+def test_smallest_grids(built, shape, npml):
+    """The smallest grids the API accepts (3 cells on an axis: one updated
+    cell between the two edges), with and without a C-PML layer."""
+    import oracle
+    from ela3d_gb300 import ShotParams, media
+
+    nx, ny, nz = shape
+    rec = np.array([[x, y, z] for x in range(nx) for y in range(ny) for z in range(nz)], np.int32)
+    p = ShotParams(nx=nx, ny=ny, nz=nz, nstep=30, dt=1e-3, npml=npml, f0=30.0, t0=0.04,
+                   src=(nx // 2, ny // 2, nz // 2), rec=rec, sampgat=1)
+    cp, cs, rho = media.anticline_layers(nx, ny, nz, depths=(1, 2, 3, 9), amp=0.5, sigma=2, seed=3)
+    seis, fields = run_gpu(p, cp, cs, rho)
+    want_s, want_f = oracle.run(p, cp, cs, rho)
+    assert np.any(want_s != 0)
+    check(seis, fields, want_s, want_f, TOL32)
