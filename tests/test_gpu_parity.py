@@ -201,3 +201,19 @@ def test_smallest_grids(built, shape, npml):
     want_s, want_f = oracle.run(p, cp, cs, rho)
     assert np.any(want_s != 0)
     check(seis, fields, want_s, want_f, TOL32)
+
+
+def test_no_samples_and_no_receivers(built):
+    """sampgat larger than nstep (no sample is ever taken) and a shot without
+    receivers: empty seismograms, the same fields as with receivers."""
+    from ela3d_gb300 import Plan
+
+    p, cp, cs, rho = small_case(nstep=12)
+    _, want_f = run_gpu(p, cp, cs, rho)
+    for q in (p.with_(sampgat=13), p.with_(rec=np.zeros((0, 3), np.int32))):
+        with Plan(q, cp, cs, rho) as plan:
+            plan.run(q.nstep)
+            s = plan.seismograms()
+            f = np.stack([plan.field(c) for c in range(9)])
+        assert s.size == 0
+        assert np.array_equal(f, want_f)
