@@ -188,7 +188,10 @@ ela3d_status ela3d_plan_info_get(ela3d_plan *plan, ela3d_plan_info *out);
  * trace so far, the step count) as one host buffer of
  * ela3d_checkpoint_size bytes.  ela3d_checkpoint_load restores it into a
  * plan created with the same parameters (in this process or another), which
- * then continues exactly as the saved plan would have.  The reference's
+ * then continues exactly as the saved plan would have; a checkpoint of a
+ * plan with other sizes, spacings, time step, C-PML coefficients, source or
+ * receivers is refused (ELA3D_ERR_INVALID_ARG).  The model travels in the
+ * checkpoint.  The reference's
  * snapshots hold vx, vy, vz only and cannot resume a run; no counterpart. */
 ela3d_status ela3d_checkpoint_size(ela3d_plan *plan, int64_t *bytes);
 ela3d_status ela3d_checkpoint_save(ela3d_plan *plan, void *buf, int64_t bytes);
