@@ -35,6 +35,11 @@ using namespace ela3d;
 
 namespace {
 
+// Running cells at which the batched kernels fill the GPU (a 256^3 shot
+// alone streams at 0.9 of the HBM roofline): below it the worker keeps
+// admitting queued requests before it waits for the device.
+constexpr double kFullCells = 16.0 * 1024 * 1024;
+
 double now_s() {
   using namespace std::chrono;
   return duration<double>(steady_clock::now().time_since_epoch()).count();
@@ -129,6 +134,17 @@ struct ela3d_server {
     for (const Callback &c : due) c.fn(c.ticket, c.status, c.user);
   }
 
+  // Cells the running shots hold.  Called with the lock held (clients add
+  // to and remove from `reqs`).
+  double running_cells() const {
+    double c = 0.0;
+    for (uint64_t t : running) {
+      const ela3d_params &q = reqs.at(t)->p;
+      c += (double)q.nx * q.ny * q.nz;
+    }
+    return c;
+  }
+
   // The next request to admit, in arrival order, taken off the queue (with
   // its device bytes booked), or null when the front request must wait for
   // memory, a slot or the fill target.  Cancelled and oversize requests at
@@ -148,11 +164,7 @@ struct ela3d_server {
         cv_done.notify_all();
         continue;
       }
-      double active_cells = 0.0;   // held by the running shots
-      for (uint64_t t : running) {
-        const ela3d_params &q = reqs[t]->p;
-        active_cells += (double)q.nx * q.ny * q.nz;
-      }
+      const double active_cells = running_cells();
       const bool slot = cfg.max_active <= 0 || (int)running.size() < cfg.max_active;
       const bool fill = cfg.fill_cells <= 0 || active_cells < (double)cfg.fill_cells;
       if (!slot || !fill || used + r.footprint > budget) return nullptr;
@@ -213,6 +225,7 @@ struct ela3d_server {
       // next boundary.  With nothing running, the first admission starts
       // the device and the others join while it works.
       for (bool any = false;;) {
+        double cells_now = 0.0;   // held by the running shots after this admission
         Request *r = nullptr;
         {
           std::lock_guard<std::mutex> g(mu);
@@ -238,9 +251,13 @@ struct ela3d_server {
             running.push_back(r->ticket);
             any = true;
           }
+          cells_now = running_cells();
           cv_done.notify_all();
         }
-        if (round > 0 ? eng->idle() : any) break;
+        // stop admitting for this round once the device has finished it --
+        // unless the running shots are still too few to fill it, in which
+        // case the next round would be small anyway
+        if ((round > 0 ? eng->idle() : any) && cells_now >= kFullCells) break;
       }
       run_callbacks();
       if (round == 0) {
