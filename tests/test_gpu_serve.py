@@ -244,3 +244,68 @@ def test_completion_callbacks_once_each_with_the_final_status(built):
     assert (got[tickets[3]], got[t_first], got[t_last], got[t_big]) == (8, 8, 8, 7)
     for q in range(3):
         assert np.array_equal(seen[tickets[q]], want[q])
+
+
+def test_randomised_clients_every_request_ends_once(built):
+    """Eight client threads, each with its own seeded script: submit
+    requests (some generated on the device), cancel some at random moments,
+    poll and read partial samples while they run, register completion
+    callbacks, wait, release.  Invariants: every request ends exactly once
+    (one callback, one final state), a request that ends done has exactly its
+    alone result, a cancelled one reports ELA3D_ERR_CANCELLED, and the
+    server's counts add up."""
+    import random
+
+    from ela3d_gb300 import Ela3dError, Server
+
+    pool = [request(s) for s in range(70, 76)]
+    want = [alone(*r) for r in pool]
+    ends, results, errors = {}, {}, []
+    lock = threading.Lock()
+
+    def on_done(t, st):
+        with lock:
+            ends.setdefault(t, []).append(st)
+
+    with Server(steps_per_round=15, variant=0, max_active=5) as srv:
+        def client(cid):
+            rnd = random.Random(cid)
+            mine = []
+            try:
+                for _ in range(4):
+                    q = rnd.randrange(len(pool))
+                    t = srv.submit(*pool[q])
+                    srv.on_done(t, on_done)
+                    mine.append((t, q, rnd.random() < 0.25))
+                    time.sleep(rnd.uniform(0, 0.01))
+                for t, q, kill in mine:
+                    if kill:
+                        srv.cancel(t)
+                    state, ready = srv.poll(t)
+                    if ready:
+                        srv.read(t, 0, ready)        # a partial read while it may still run
+                for t, q, kill in mine:
+                    try:
+                        srv.wait(t)
+                        with lock:
+                            results[t] = (q, srv.read(t))
+                    except Ela3dError as e:
+                        assert kill and e.status == 8, (t, e.status)
+                    srv.release(t)
+            except Exception as e:  # reported to the main thread
+                errors.append(repr(e))
+
+        th = [threading.Thread(target=client, args=(c,)) for c in range(8)]
+        for x in th:
+            x.start()
+        for x in th:
+            x.join()
+        st = srv.stats()
+    assert not errors, errors
+    assert len(ends) == 32 and all(len(v) == 1 for v in ends.values())
+    done = [t for t, v in ends.items() if v[0] == 0]
+    assert sorted(done) == sorted(results)
+    assert all(v[0] in (0, 8) for v in ends.values())
+    for t, (q, seis) in results.items():
+        assert np.array_equal(seis, want[q]), t
+    assert st["submitted"] == 32 and st["completed"] + st["cancelled"] == 32 and st["failed"] == 0
