@@ -217,3 +217,36 @@ def test_no_samples_and_no_receivers(built):
             f = np.stack([plan.field(c) for c in range(9)])
         assert s.size == 0
         assert np.array_equal(f, want_f)
+
+
+def test_plans_in_concurrent_threads(built):
+    """One plan per thread, four threads at once on the same device (each
+    plan owns its streams and memory): every plan's results equal the same
+    plan run alone."""
+    import threading
+
+    from ela3d_gb300 import Plan
+
+    cases = [small_case(nstep=40, src=(10 + 5 * q, 17, 23)) for q in range(4)]
+    want = [run_gpu(*c) for c in cases]
+    got = [None] * 4
+    errors = []
+
+    def worker(q):
+        try:
+            p, cp, cs, rho = cases[q]
+            with Plan(p, cp, cs, rho) as plan:
+                for _ in range(4):
+                    plan.run(10)
+                got[q] = (plan.seismograms(), np.stack([plan.field(c) for c in range(9)]))
+        except Exception as e:
+            errors.append(repr(e))
+
+    th = [threading.Thread(target=worker, args=(q,)) for q in range(4)]
+    for x in th:
+        x.start()
+    for x in th:
+        x.join()
+    assert not errors, errors
+    for q in range(4):
+        assert np.array_equal(got[q][0], want[q][0]) and np.array_equal(got[q][1], want[q][1]), q
