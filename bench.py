@@ -392,6 +392,8 @@ def run_ours(args, rank, world, local):
     roof["step_frac"] = roof["step_achieved_gbs"] / peak
 
     extra = {}
+    if args.large > 0 and rank == 0:
+        extra["large_grid"] = large_grid(args.large)
     if not args.no_batched:
         extra["batched"] = batched_shots(args, value)   # shots split across ranks
         if world == 1:
@@ -422,6 +424,32 @@ def run_ours(args, rank, world, local):
                 "cpu_baseline": cpu, "reference_gpu_program": ref_gpu, "clocks": clk, "accuracy": accuracy}
         line.update(extra)
         print(json.dumps(line), flush=True)
+
+
+def large_grid(n: int, steps: int = 100) -> dict:
+    """One n^3 shot of the same anticline, its model generated on the device
+    (no host arrays): the single-shot rate where the C-PML layers are a
+    smaller share of the cells (off by default: --large N)."""
+    import ela3d_gb300 as E
+    from ela3d_gb300 import media
+    from ela3d_gb300.metrics import bytes_per_cell
+
+    npml, f0 = 16, 12.0
+    p = E.ShotParams(nx=n, ny=n, nz=n, nstep=steps + 20, dt=1e-3, npml=npml, f0=f0, t0=1.2 / f0, factor=1e7,
+                     stf=0, src_kind=0, src=(n // 2, n // 2, npml + 3), src_w=(0.0, 0.0, 1.0), sampgat=1,
+                     rec=np.array([[x, n // 2, npml + 3] for x in range(n // 2 - 100, n // 2 + 101)], np.int32))
+    with E.Plan.from_model(p, media.anticline_256_spec(n)) as plan:
+        plan.run(20)
+        ms = plan.run_timed(steps)
+        info = plan.info()
+    cells = p.cells
+    bpc = bytes_per_cell(n, n, n, npml)["step"]
+    peak, _ = measured_peaks()
+    value = cells * steps / (ms / 1e3) / 1e9
+    return {"workload": f"{n}^3 anticline (16 PML cells), model generated on the GPU, FP32", "metric": METRIC,
+            "value": value, "steps_timed": steps, "ms_per_step": ms / steps, "bytes_per_cell_update": bpc,
+            "frac_of_hbm": value * 1e9 * bpc / 1e9 / peak, "device_bytes": int(info.device_bytes),
+            "timing": "CUDA events around replayed 50-step graphs, built-in kernel choice"}
 
 
 def batched_shots(args, single_value: float) -> dict:
@@ -667,6 +695,8 @@ def main():
     ap.add_argument("--prefetch", type=int, default=-1,
                     help="C-PML memory-variable prefetch mode of the single-shot plan (ela3d_tuning.prefetch: "
                          "0 none, 2 x slab into L1, 6 also y/z slabs into L2); -1 = tuned or built-in")
+    ap.add_argument("--large", type=int, default=0,
+                    help="also time one N^3 anticline shot generated on the GPU (e.g. 1024; off by default)")
     ap.add_argument("--variant", type=int, default=-1,
                     help="kernel variant (tile shape, stages) of the single-shot plan, an index of "
                          "ela3d_gb300.variants(); -1 = tuned or built-in")

@@ -186,7 +186,8 @@ TuneChoice default_choice(int fp64, int nx, int ny, int nz) {
   int n = 0;
   const Variant *v = variants(&n);
   // first variant of the precision (the list is ordered best first for
-  // large grids), z-chunks of 10 planes dealt round-robin, both prefetches;
+  // large grids), z-chunks of 10 planes (more for wide grids, below) dealt
+  // round-robin, both prefetches;
   // a grid too small to give every SM several chunks gets equal contiguous
   // shares instead (round-robin would leave some blocks with one chunk more)
   int i = 0;
@@ -197,6 +198,17 @@ TuneChoice default_choice(int fp64, int nx, int ny, int nz) {
     int dev = 0, sms = 152;
     if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const long long tiles = (long long)((nx + v[i].tx - 1) / v[i].tx) * ((ny + v[i].ty - 1) / v[i].ty);
+    // with more tiles per plane than blocks, the blocks running together no
+    // longer hold neighbouring chunks of one tile column, so each chunk's
+    // look-ahead and z-1 planes come from DRAM again: longer chunks keep
+    // that share small (measured: 512^3 best at 16-32 planes, 1024^3 at
+    // 64-128), as long as every block still gets several of them
+    if (tiles > sms) {
+      int ch = 16;
+      while (ch < 128 && ch * sms < 16 * tiles) ch *= 2;
+      while (ch > 10 && tiles * ((nz + ch - 1) / ch) < 8ll * sms) ch /= 2;
+      c.chunk = std::max(10, ch);
+    }
     const long long chunks = tiles * ((nz + c.chunk - 1) / c.chunk);
     if (chunks < 8ll * std::max(1, sms)) c.kind = 0;
     // a shot whose twelve arrays fit in L2 gains nothing from bringing its

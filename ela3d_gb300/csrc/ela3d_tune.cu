@@ -107,13 +107,13 @@ void tune_store(const std::vector<ela3d_params> &ps, const TuneChoice &c) {
 }
 
 // Candidate schedules and prefetch modes for a workload: contiguous shares;
-// z-chunks of 6..32 planes round-robin; for batches also shot-interleaved
+// z-chunks of 6..128 planes round-robin; for batches also shot-interleaved
 // chunks; each with both memory-variable prefetches or the x slab's only.
 static std::vector<TuneChoice> schedules(int nshots) {
   std::vector<TuneChoice> v;
   for (int pf : {kPrefetchDefault, (int)CTL_PF_X}) {
     v.push_back({0, 0, 16, 0, pf});
-    for (int ch : {6, 8, 10, 12, 16, 32}) v.push_back({0, 1, ch, 0, pf});
+    for (int ch : {6, 8, 10, 12, 16, 32, 64, 128}) v.push_back({0, 1, ch, 0, pf});
     if (nshots > 1)
       for (int ch : {8, 16}) v.push_back({0, 2, ch, 0, pf});
   }
