@@ -26,7 +26,8 @@ Also in the same line: "batched" (64 shots of the 256^3 anticline sharing
 one model, advanced together), "uneven" (48 uneven grids together vs one
 at a time) and "serving" (a Poisson request stream swept to saturation,
 p50/p99 latency), each next to the single-shot path on the same GPU, each
-with an FP64 re-run of sampled shots (fp64_check).
+with an FP64 re-run of sampled shots (fp64_check); and "large_grid" (one
+512^3 shot, its model generated on the GPU).
 Reference arm (--impl reference): the reference CPU program itself on all
 host cores (one process per core, each a bounded sample of the same shot),
 rank 0 only.
@@ -392,7 +393,7 @@ def run_ours(args, rank, world, local):
     roof["step_frac"] = roof["step_achieved_gbs"] / peak
 
     extra = {}
-    if args.large > 0 and rank == 0:
+    if args.large > 0 and rank == 0 and not args.no_batched:
         extra["large_grid"] = large_grid(args.large)
     if not args.no_batched:
         extra["batched"] = batched_shots(args, value)   # shots split across ranks
@@ -429,7 +430,7 @@ def run_ours(args, rank, world, local):
 def large_grid(n: int, steps: int = 100) -> dict:
     """One n^3 shot of the same anticline, its model generated on the device
     (no host arrays): the single-shot rate where the C-PML layers are a
-    smaller share of the cells (off by default: --large N)."""
+    smaller share of the cells (--large N; 0 turns it off)."""
     import ela3d_gb300 as E
     from ela3d_gb300 import media
     from ela3d_gb300.metrics import bytes_per_cell
@@ -690,13 +691,14 @@ def main():
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end shot (short profiling runs)")
     ap.add_argument("--no-accuracy", action="store_true",
                     help="skip the FP64 re-run of the end-to-end shot (accuracy of every seismogram and field)")
-    ap.add_argument("--no-batched", action="store_true", help="skip the batched and uneven workloads")
+    ap.add_argument("--no-batched", action="store_true",
+                    help="skip the batched, uneven, serving and larger-grid workloads")
     ap.add_argument("--no-autotune", action="store_true", help="use the built-in kernel choice")
     ap.add_argument("--prefetch", type=int, default=-1,
                     help="C-PML memory-variable prefetch mode of the single-shot plan (ela3d_tuning.prefetch: "
                          "0 none, 2 x slab into L1, 6 also y/z slabs into L2); -1 = tuned or built-in")
-    ap.add_argument("--large", type=int, default=0,
-                    help="also time one N^3 anticline shot generated on the GPU (e.g. 1024; off by default)")
+    ap.add_argument("--large", type=int, default=512,
+                    help="also time one N^3 anticline shot generated on the GPU (0: off)")
     ap.add_argument("--variant", type=int, default=-1,
                     help="kernel variant (tile shape, stages) of the single-shot plan, an index of "
                          "ela3d_gb300.variants(); -1 = tuned or built-in")
