@@ -50,6 +50,7 @@ SIGNATURES = [
     ("ela3d_plan_destroy", _c.c_int, [_P]),
     ("ela3d_plan_inject_timeout", _c.c_int, [_P, _c.c_int32]),
     ("ela3d_plan_poison_padding", _c.c_int, [_P, _c.c_double]),
+    ("ela3d_plan_get_profiles", _c.c_int, [_P, _c.c_int32, _c.c_void_p]),
     ("ela3d_plan_check_guards", _c.c_int, [_P]),
     ("ela3d_select_device", _c.c_int, [_c.c_int32]),
     ("ela3d_run_timed", _c.c_int, [_P, _c.c_int32, _c.POINTER(_c.c_double)]),
@@ -326,6 +327,15 @@ class Plan:
         _check(self._lib.ela3d_get_kernel_timing(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(na),
                                                  ctypes.byref(nb)), "ela3d_get_kernel_timing")
         return a.value, b.value, na.value, nb.value
+
+    def profiles(self, axis: int) -> dict:
+        """The C-PML profiles of one axis as the kernels read them
+        (ela3d_plan_get_profiles): a, b, K, a_half, b_half, K_half."""
+        n = (self.params.nx, self.params.ny, self.params.nz)[axis]
+        out = np.zeros(6 * n, np.float64)
+        _check(self._lib.ela3d_plan_get_profiles(self._h, axis, out.ctypes.data), "ela3d_plan_get_profiles")
+        v = out.reshape(6, n)
+        return {"a": v[0], "b": v[1], "K": 1.0 / v[2], "a_half": v[3], "b_half": v[4], "K_half": 1.0 / v[5]}
 
     def poison_padding(self, value: float = float("nan")) -> None:
         """Test hook: `value` into every padding column of the fields and

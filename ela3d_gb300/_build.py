@@ -1,16 +1,12 @@
-"""Build recipe: nvcc for the CUDA library, gcc for the oracle.
+"""Build recipe for the CUDA library.
 
 ``build_library()`` compiles every translation unit under ``csrc/`` for
 sm_103a in parallel and links ``_build/libela3d.so`` (in-tree, git-ignored).
-``build_oracle()`` compiles the CPU restatement under ``oracle/`` and, when
-the patched reference source is present (generated by oracle/make_ref.py),
-the reference program itself.  Rebuilds only when a source is newer than the
-output.
+Rebuilds only when a source is newer than the output.
 """
 from __future__ import annotations
 
 import glob
-import shutil
 import os
 import subprocess
 import sys
@@ -20,9 +16,6 @@ ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 OUT = os.path.join(PKG, "_build")
 LIB = os.path.join(OUT, "libela3d.so")
-ORACLE_DIR = os.path.join(ROOT, "oracle")
-ORACLE_OUT = os.path.join(ORACLE_DIR, "_build")
-ORACLE_LIB = os.path.join(ORACLE_OUT, "libela3d_oracle.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2"]
@@ -70,43 +63,5 @@ def build_library(verbose: bool = False) -> str:
     return LIB
 
 
-def build_oracle() -> str:
-    os.makedirs(ORACLE_OUT, exist_ok=True)
-    srcs = [os.path.join(ORACLE_DIR, f) for f in ("ela3d_oracle.c", "ela3d_oracle_impl.h", "ela3d_oracle.h")]
-    if _newer(srcs, ORACLE_LIB):
-        subprocess.run(["gcc", "-O2", "-ffp-contract=off", "-shared", "-fPIC", srcs[0], "-o", ORACLE_LIB, "-lm"],
-                       check=True)
-    return ORACLE_LIB
-
-
-def build_reference() -> list[str]:
-    """Patched reference program (oracle/_ref); empty list when unavailable."""
-    sys.path.insert(0, ORACLE_DIR)
-    try:
-        import make_ref  # type: ignore
-    finally:
-        sys.path.pop(0)
-    ref_src = os.path.join(make_ref.DEFAULT_REF_DIR, make_ref.REF_NAME)
-    if os.path.exists(ref_src):
-        make_ref.generate(make_ref.DEFAULT_REF_DIR)
-    outs, procs = [], []
-    jobs = [(os.path.join(make_ref.OUT, f"ref_{v}.cpp"), os.path.join(make_ref.OUT, f"ref_{v}"),
-             make_ref.compiler_cmd) for v in ("f32", "f64")]
-    if shutil.which("nvcc"):   # the reference's FP32 GPU program, a timing baseline
-        jobs.append((os.path.join(make_ref.OUT, "ref_gpu_f32.cu"), os.path.join(make_ref.OUT, "ref_gpu_f32"),
-                     make_ref.gpu_compiler_cmd))
-    for src, exe, cmd in jobs:
-        if os.path.exists(src):
-            if _newer([src, os.path.join(ORACLE_DIR, "ref_harness.h")], exe):
-                procs.append((exe, subprocess.Popen(cmd(src, exe))))
-            outs.append(exe)
-    for exe, p in procs:
-        if p.wait() != 0:
-            raise RuntimeError(f"building {exe} failed")
-    return outs
-
-
 if __name__ == "__main__":
     print(build_library(verbose=True))
-    print(build_oracle())
-    print(build_reference())

@@ -123,16 +123,31 @@ __global__ void explosive_kernel(const ShotDesc<T> *shots, int nshots, int tick,
 // Kinetic 1/2 rho |v|^2 plus isotropic strain energy
 // (1/(4mu)) sigma:sigma - lambda / (4mu(3lambda+2mu)) tr(sigma)^2, cell-local,
 // accumulated in FP64 (no counterpart in the reference; the stability monitor).
+// Two passes in a fixed order, so repeated calls on one state agree to the
+// bit: one block per z-plane writes the plane's sum to part[k], then one
+// block adds the planes in order (energy_sum_kernel).
+__device__ __forceinline__ double block_sum_f64(double v) {
+  __shared__ double part[32];
+  for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+  if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = v;
+  __syncthreads();
+  v = 0.0;
+  if (threadIdx.x < 32) {
+    v = threadIdx.x < (blockDim.x >> 5) ? part[threadIdx.x] : 0.0;
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+  }
+  return v;  // valid in thread 0
+}
+
 template <typename T>
-__global__ void energy_kernel(const ShotDesc<T> *shot, int nx, int ny, int nz, double *out) {
+__global__ void energy_plane_kernel(const ShotDesc<T> *shot, int nx, int ny, double *part) {
   const ShotDesc<T> &sd = *shot;
-  const long long n = (long long)nx * ny * nz;
+  const int k = blockIdx.x;
+  const long long cells = (long long)nx * ny;
   double acc = 0.0;
-  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n;
-       q += (long long)gridDim.x * blockDim.x) {
-    const int x = (int)(q % nx);
-    const long long r = q / nx;
-    const long long o = r * sd.px + x;
+  for (long long q = threadIdx.x; q < cells; q += blockDim.x) {
+    const long long y = q / nx, x = q - y * nx;
+    const long long o = ((long long)k * ny + y) * sd.px + x;
     const double rho = sd.rho[o], cp = sd.cp[o], cs = sd.cs[o];
     const double mu = rho * cs * cs, lam = rho * (cp * cp - 2.0 * cs * cs);
     const double vx = sd.f[0][o], vy = sd.f[1][o], vz = sd.f[2][o];
@@ -148,16 +163,17 @@ __global__ void energy_kernel(const ShotDesc<T> *shot, int nx, int ny, int nz, d
     }
     acc += e;
   }
-  for (int off = 16; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
-  __shared__ double part[32];
-  if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = acc;
-  __syncthreads();
-  if (threadIdx.x < 32) {
-    acc = threadIdx.x < (blockDim.x >> 5) ? part[threadIdx.x] : 0.0;
-    for (int off = 16; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
-    if (threadIdx.x == 0) atomicAdd(out, acc * (double)(1.0 / sd.idx) * (double)(1.0 / sd.idy) *
-                                              (double)(1.0 / sd.idz));
-  }
+  acc = block_sum_f64(acc);
+  if (threadIdx.x == 0) part[k] = acc;
+}
+
+template <typename T>
+__global__ void energy_sum_kernel(const ShotDesc<T> *shot, const double *part, int nz, double *out) {
+  const ShotDesc<T> &sd = *shot;
+  double acc = 0.0;
+  for (int k = threadIdx.x; k < nz; k += blockDim.x) acc += part[k];
+  acc = block_sum_f64(acc);
+  if (threadIdx.x == 0) *out = acc * (double)(1.0 / sd.idx) * (double)(1.0 / sd.idy) * (double)(1.0 / sd.idz);
 }
 
 // Device step counter for replayable CUDA graphs.
@@ -213,13 +229,20 @@ cudaError_t launch_explosive_f64(const ShotDesc<double> *shots, int nshots, int 
   explosive_kernel<double><<<(nshots + 63) / 64, 64, 0, s>>>(shots, nshots, tick, dtick);
   return cudaGetLastError();
 }
-cudaError_t launch_energy_f32(const ShotDesc<float> *shot, int nx, int ny, int nz, double *out, cudaStream_t s) {
-  energy_kernel<float><<<blocks_for((long long)nx * ny * nz, 256, 1216), 256, 0, s>>>(shot, nx, ny, nz, out);
+// out[0] = the energy; out[1 .. nz] = the per-plane sums (scratch)
+template <typename T>
+static cudaError_t launch_energy(const ShotDesc<T> *shot, int nx, int ny, int nz, double *out, cudaStream_t s) {
+  energy_plane_kernel<T><<<nz, 256, 0, s>>>(shot, nx, ny, out + 1);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  energy_sum_kernel<T><<<1, 256, 0, s>>>(shot, out + 1, nz, out);
   return cudaGetLastError();
 }
+cudaError_t launch_energy_f32(const ShotDesc<float> *shot, int nx, int ny, int nz, double *out, cudaStream_t s) {
+  return launch_energy(shot, nx, ny, nz, out, s);
+}
 cudaError_t launch_energy_f64(const ShotDesc<double> *shot, int nx, int ny, int nz, double *out, cudaStream_t s) {
-  energy_kernel<double><<<blocks_for((long long)nx * ny * nz, 256, 1216), 256, 0, s>>>(shot, nx, ny, nz, out);
-  return cudaGetLastError();
+  return launch_energy(shot, nx, ny, nz, out, s);
 }
 
 }  // namespace ela3d

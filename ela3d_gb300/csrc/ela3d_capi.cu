@@ -362,6 +362,11 @@ ela3d_status ela3d_plan_check_guards(ela3d_plan *plan) {
   return plan->eng->check_guards();
 }
 
+ela3d_status ela3d_plan_get_profiles(ela3d_plan *plan, int32_t axis, double *out) {
+  if (!plan) return ELA3D_ERR_INVALID_ARG;
+  return plan->eng->profiles(0, axis, out);
+}
+
 ela3d_status ela3d_plan_poison_padding(ela3d_plan *plan, double value) {
   if (!plan) return ELA3D_ERR_INVALID_ARG;
   return plan->eng->poison_padding(value);

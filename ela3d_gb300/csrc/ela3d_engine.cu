@@ -328,7 +328,6 @@ class Engine final : public EngineBase {
     CK(cudaStreamCreateWithFlags(&setup_, cudaStreamNonBlocking));
     CK(cudaMalloc(&d_err_, sizeof(unsigned)));
     CK(cudaMemset(d_err_, 0, sizeof(unsigned)));
-    CK(cudaMalloc(&d_energy_, sizeof(double)));
     CK(cudaMalloc(&d_tick_, sizeof(int)));
     CK(cudaMemset(d_tick_, 0, sizeof(int)));
     // ELA3D_PSI_PREFETCH=<bits> overrides the tuned prefetch mode (experiments)
@@ -1087,12 +1086,34 @@ class Engine final : public EngineBase {
   ela3d_status energy(int shot, double *out) override {
     if (shot < 0 || shot >= nshots() || !out) BAD("bad shot or output");
     const Shot<T> &s = *shots_[shot];
-    CK(cudaMemsetAsync(d_energy_, 0, sizeof(double), stream_));
     const ShotDesc<T> *dd = d_desc_ ? d_desc_ + shot : nullptr;
     if (!dd) BAD("engine not finalized");
+    // the result and one partial sum per plane (grown to the largest nz seen)
+    if (energy_cap_ < s.d.nz + 1) {
+      CK(cudaStreamSynchronize(stream_));
+      if (d_energy_) cudaFree(d_energy_);
+      d_energy_ = nullptr;
+      energy_cap_ = 0;
+      CK(cudaMalloc(&d_energy_, sizeof(double) * (size_t)(s.d.nz + 1)));
+      energy_cap_ = s.d.nz + 1;
+    }
     CK(Fp<T>::energy(dd, s.d.nx, s.d.ny, s.d.nz, d_energy_, stream_));
     CK(cudaMemcpyAsync(out, d_energy_, sizeof(double), cudaMemcpyDeviceToHost, stream_));
     CK(cudaStreamSynchronize(stream_));
+    return ELA3D_OK;
+  }
+
+  ela3d_status profiles(int shot, int axis, double *out) override {
+    if (shot < 0 || shot >= nshots() || !out || axis < 0 || axis > 2) BAD("bad shot, axis or output");
+    const Shot<T> &s = *shots_[shot];
+    const int n = axis == 0 ? s.d.nx : axis == 1 ? s.d.ny : s.d.nz;
+    const int stride = axis == 0 ? s.px : n;
+    const size_t off = axis == 0 ? 0 : axis == 1 ? 6 * (size_t)s.px : 6 * (size_t)(s.px + s.d.ny);
+    std::vector<T> h(6 * (size_t)stride);
+    CK(cudaMemcpyAsync(h.data(), s.prof + off, h.size() * sizeof(T), cudaMemcpyDeviceToHost, stream_));
+    CK(cudaStreamSynchronize(stream_));
+    for (int q = 0; q < 6; ++q)
+      for (int i = 0; i < n; ++i) out[(size_t)q * n + i] = (double)h[(size_t)q * stride + i];
     return ELA3D_OK;
   }
 
@@ -1276,6 +1297,7 @@ class Engine final : public EngineBase {
   int2 *d_ranges_ = nullptr;
   unsigned *d_err_ = nullptr;
   double *d_energy_ = nullptr;
+  int energy_cap_ = 0;   // doubles held by d_energy_
   int nblocks_ = 0, nitems_ = 0, per_sm_ = 1;
   size_t items_cap_ = 0, ranges_cap_ = 0;
   std::vector<int> sched_key_;

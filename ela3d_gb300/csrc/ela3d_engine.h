@@ -91,6 +91,9 @@ class EngineBase {
   virtual ela3d_status checkpoint_save(void *buf, int64_t bytes) = 0;
   virtual ela3d_status checkpoint_load(const void *buf, int64_t bytes) = 0;
   virtual ela3d_status energy(int shot, double *out) = 0;
+  // The shot's C-PML profiles of one axis as stored on the device, in
+  // double: a, b, 1/K, a_half, b_half, 1/K_half, n values each (test hook).
+  virtual ela3d_status profiles(int shot, int axis, double *out) = 0;
   virtual ela3d_status info(int shot, ela3d_plan_info *out) = 0;
   virtual ela3d_status set_timing(bool on) = 0;
   virtual ela3d_status inject_timeout(int launches) = 0;

@@ -16,10 +16,10 @@
 // Calls that overlap in time on one device (other streams, other host
 // threads) share that array and race with each other; serialise them.
 //
-// The scratch address is looked up once per device (cudaGetSymbolAddress,
-// with that device current) on the first call made there.  If you capture
-// work into a CUDA graph, make that first call on each device before the
-// capture begins.
+// The scratch address is looked up (cudaGetSymbolAddress, on the current
+// device) at every call; the first call on a device is its set-up, which
+// also loads the library's kernels there.  If you capture work into a CUDA
+// graph, make that first call on each device before the capture begins.
 //
 // Energy per cell, accumulated in FP64 (the same definition as the plan's
 // stability monitor): 1/2 rho |v|^2 + (1/(4 mu)) sigma:sigma
@@ -28,14 +28,12 @@
 // in plane order by one block, so repeated calls give identical results.
 #include <cuda_runtime.h>
 
-#include <mutex>
 #include <string>
 
 #include "ela3d_engine.h"
 
 namespace {
 constexpr int kNoAllocMaxPlanes = 16384;
-constexpr int kNoAllocMaxDevices = 64;
 constexpr int kNoAllocThreads = 256;
 }  // namespace
 
@@ -68,10 +66,11 @@ __device__ __forceinline__ double block_sum(double v, double *part) {
 __global__ void __launch_bounds__(kNoAllocThreads) plane_energy_kernel(NoAllocFields a, double *plane_sum) {
   __shared__ double part[kNoAllocThreads / 32];
   const int k = blockIdx.x;
-  const int cells = a.nx * a.ny;
+  // 64-bit cell index: nx * ny may come within a block's stride of 2^31
+  const long long cells = (long long)a.nx * a.ny;
   double acc = 0.0;
-  for (int q = threadIdx.x; q < cells; q += blockDim.x) {
-    const int x = q % a.nx, y = q / a.nx;
+  for (long long q = threadIdx.x; q < cells; q += blockDim.x) {
+    const long long y = q / a.nx, x = q - y * a.nx;
     const long long o = ((long long)k * a.ny + y) * a.pitch + x;
     const double rho = a.rho[o], cp = a.cp[o], cs = a.cs[o];
     const double mu = rho * cs * cs, lam = rho * (cp * cp - 2.0 * cs * cs);
@@ -102,28 +101,16 @@ __global__ void __launch_bounds__(kNoAllocThreads) sum_planes_kernel(const doubl
   if (threadIdx.x == 0) *out = acc * volume;
 }
 
-std::mutex g_noalloc_mu;
-double *g_noalloc_scratch[kNoAllocMaxDevices] = {};
-
-// The scratch array's device address on the current device, looked up on
-// the first call made with that device current.
+// The scratch array's device address on the current device.  It is looked
+// up on every call (cudaGetSymbolAddress allocates nothing), so a device or
+// context reset, after which the library's module is loaded again and the
+// array may sit elsewhere, needs no special care.  The first call on a
+// device also loads the library's kernels there.
 ela3d_status noalloc_scratch(double **out) {
-  int dev = -1;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) return status_from_cuda(e, "cudaGetDevice");
-  if (dev < 0 || dev >= kNoAllocMaxDevices) {
-    set_last_error("ela3d_energy_noalloc: device ordinal " + std::to_string(dev) + " beyond the " +
-                   std::to_string(kNoAllocMaxDevices) + " it keeps scratch addresses for");
-    return ELA3D_ERR_INVALID_ARG;
-  }
-  std::lock_guard<std::mutex> g(g_noalloc_mu);
-  if (!g_noalloc_scratch[dev]) {
-    void *p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_noalloc_plane_energy);
-    if (e != cudaSuccess) return status_from_cuda(e, "cudaGetSymbolAddress");
-    g_noalloc_scratch[dev] = static_cast<double *>(p);
-  }
-  *out = g_noalloc_scratch[dev];
+  void *p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_plane_energy);
+  if (e != cudaSuccess) return status_from_cuda(e, "cudaGetSymbolAddress");
+  *out = static_cast<double *>(p);
   return ELA3D_OK;
 }
 

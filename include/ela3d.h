@@ -176,9 +176,11 @@ ela3d_status ela3d_energy(ela3d_plan *plan, double *out);
  * synchronisation).  Its intermediate sums live in a fixed array inside the
  * library: nz <= 16384 (a larger nz returns ELA3D_ERR_INVALID_ARG), nothing
  * in it needs to start at zero, and calls overlapping in time on one device
- * race for it -- serialise them.  The first call on a device looks up the
- * array's address; when capturing work into a CUDA graph, make that first
- * call before the capture begins.  No counterpart in the reference. */
+ * race for it -- serialise them.  Every call looks up the array's address
+ * on the current device; the first call on a device is its set-up (it also
+ * loads the library's kernels there), so when capturing work into a CUDA
+ * graph, make that first call before the capture begins.  No counterpart in
+ * the reference. */
 ela3d_status ela3d_energy_noalloc(const float *const *fields, const float *cp, const float *cs,
                                   const float *rho, int32_t nx, int32_t ny, int32_t nz, int32_t pitch_x,
                                   double dx, double dy, double dz, double *out, void *stream);
@@ -213,6 +215,11 @@ ela3d_status ela3d_plan_inject_timeout(ela3d_plan *plan, int32_t steps);
  * x in [nx, pitch_x) of the nine fields and of the C-PML memory-variable
  * arrays -- cells no update may read into the grid.  No counterpart. */
 ela3d_status ela3d_plan_poison_padding(ela3d_plan *plan, double value);
+/* Test hook: the plan's C-PML profiles of one axis (0 = x, 1 = y, 2 = z)
+ * as the kernels read them, widened to double: a, b, 1/K, a_half, b_half,
+ * 1/K_half, n values each (n = nx, ny or nz), so 6n values into `out`.
+ * Checked against the reference's profile code (simpelmodel.cpp:142-361). */
+ela3d_status ela3d_plan_get_profiles(ela3d_plan *plan, int32_t axis, double *out);
 /* Debug check: with the environment variable ELA3D_GUARD_ZONES=<bytes> set
  * when a plan is created, every array in its device pool is followed (and
  * the pool preceded) by a zone of that many bytes filled with 0xA5; this

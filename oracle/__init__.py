@@ -43,12 +43,8 @@ class OracleParams(ctypes.Structure):
 def load():
     global _LIB
     if _LIB is None:
-        import sys
-        sys.path.insert(0, os.path.dirname(HERE))
-        try:
-            from ela3d_gb300._build import build_oracle
-        finally:
-            sys.path.pop(0)
+        from .build import build_oracle
+
         lib = ctypes.CDLL(build_oracle())
         for name in ("oracle_run_f32", "oracle_run_f64"):
             getattr(lib, name).restype = ctypes.c_int

@@ -41,6 +41,8 @@ Its kernels' indices were checked by reading for cubic grids whose edge is a
 multiple of 8: every neighbour access stays inside the arrays.
 
 Usage: python oracle/make_ref.py [--ref DIR] [--no-build]
+(DIR defaults to ELA3D_REFERENCE_DIR, else a ``reference`` directory beside
+this repository.)
 """
 from __future__ import annotations
 
@@ -55,7 +57,18 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
 REF_NAME = "seismicCPML_3d_isotropic_simpelmodel.cpp"
 GPU_REF_NAME = "seismicCPML_3d_isotropic_cudazerocopy.cu"
-DEFAULT_REF_DIR = "/root/reference"
+
+
+def reference_dir() -> str | None:
+    """The reference checkout: ``ELA3D_REFERENCE_DIR`` when set, else a
+    ``reference`` directory beside this repository; None when neither holds
+    the reference source."""
+    cands = [os.environ.get("ELA3D_REFERENCE_DIR"),
+             os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")]
+    for c in cands:
+        if c and os.path.exists(os.path.join(c, REF_NAME)):
+            return c
+    return None
 
 
 def _sub(src: str, old: str, new: str, count: int = 1) -> str:
@@ -194,23 +207,29 @@ def compiler_cmd(src: str, exe: str) -> list[str]:
             "-I", OUT, "-I", HERE, src, "-o", exe]
 
 
+def _write_if_changed(path: str, text: str) -> None:
+    """Leaves an identical file alone, so that its binary is not rebuilt."""
+    if os.path.exists(path):
+        with open(path, "r") as f:
+            if f.read() == text:
+                return
+    with open(path, "w") as f:
+        f.write(text)
+
+
 def generate(ref_dir: str) -> None:
     with open(os.path.join(ref_dir, REF_NAME), "r", encoding="latin-1") as f:
         src = f.read()
     os.makedirs(OUT, exist_ok=True)
     p32 = patch(src)
-    with open(os.path.join(OUT, "ref_f32.cpp"), "w") as f:
-        f.write(p32)
-    with open(os.path.join(OUT, "ref_f64.cpp"), "w") as f:
-        f.write(to_f64(p32))
-    with open(os.path.join(OUT, "conio.h"), "w") as f:
-        f.write("/* empty stand-in for the Windows console header */\n")
+    _write_if_changed(os.path.join(OUT, "ref_f32.cpp"), p32)
+    _write_if_changed(os.path.join(OUT, "ref_f64.cpp"), to_f64(p32))
+    _write_if_changed(os.path.join(OUT, "conio.h"), "/* empty stand-in for the Windows console header */\n")
     gpu = os.path.join(ref_dir, GPU_REF_NAME)
     if os.path.exists(gpu):
         with open(gpu, "r", encoding="latin-1") as f:
             g = patch_gpu(f.read())
-        with open(os.path.join(OUT, "ref_gpu_f32.cu"), "w") as f:
-            f.write(g)
+        _write_if_changed(os.path.join(OUT, "ref_gpu_f32.cu"), g)
 
 
 def build() -> list[str]:
@@ -236,11 +255,12 @@ def build() -> list[str]:
 
 def main() -> int:
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default=DEFAULT_REF_DIR)
+    ap.add_argument("--ref", default=None)
     ap.add_argument("--no-build", action="store_true")
     a = ap.parse_args()
-    if os.path.exists(os.path.join(a.ref, REF_NAME)):
-        generate(a.ref)
+    ref = a.ref or reference_dir()
+    if ref and os.path.exists(os.path.join(ref, REF_NAME)):
+        generate(ref)
     elif not os.path.exists(os.path.join(OUT, "ref_f32.cpp")):
         print("reference source not found and no patched copy present", file=sys.stderr)
         return 1

@@ -10,6 +10,9 @@ slices of every final field (the x-y plane through the source depth and the
 y-z plane through the source x).
 
 Run from the repository root:  python tests/golden/make_golden.py
+The full-size workloads (``ref_homogeneous_101_full.npz``,
+``ref_anticline_256_full.npz``) take about half an hour of CPU and are made
+separately:  python tests/golden/make_golden.py --full [name ...]
 """
 from __future__ import annotations
 
@@ -83,9 +86,63 @@ def params_json(p) -> str:
     return json.dumps(d)
 
 
+def full_cases():
+    """The two benchmark workloads at their full sizes: the 101^3 homogeneous
+    cube for its 1000 steps, and the 256^3 anticline shot for its 2000 steps
+    with its 201-receiver line (a quarter of an hour of CPU per precision)."""
+    return {
+        "homogeneous_101_full": configs.homogeneous_101(),
+        "anticline_256_full": configs.anticline_256(),
+    }
+
+
+def main_full(names=None):
+    """Runs the reference program on the full-size workloads, both precisions
+    in parallel.  The float32 seismograms are kept whole; the float64 ones,
+    which check the FP64 build, are kept for every fourth receiver of lines
+    longer than 64 receivers (the file stays a few MB)."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    import oracle
+
+    if oracle.reference_binary(False) is None or oracle.reference_binary(True) is None:
+        raise SystemExit("build the reference program first: python oracle/make_ref.py")
+    todo = {k: v for k, v in full_cases().items() if names is None or k in names}
+
+    def one(job):
+        name, fp64 = job
+        p, cp, cs, rho = todo[name]
+        seis, fields, secs, _ = oracle.run_reference(p, cp, cs, rho, fp64=fp64)
+        return name, fp64, seis, summarize(p, fields), secs
+
+    jobs = [(n, f) for n in todo for f in (False, True)]
+    results = {}
+    with ThreadPoolExecutor(len(jobs)) as ex:
+        for name, fp64, seis, summ, secs in ex.map(one, jobs):
+            results[(name, fp64)] = (seis, summ)
+            print(name, "f64" if fp64 else "f32", f"{secs:.0f} s", flush=True)
+    for name, (p, cp, cs, rho) in todo.items():
+        out = {"params": np.array(params_json(p))}
+        for fp64 in (False, True):
+            seis, summ = results[(name, fp64)]
+            tag = "f64" if fp64 else "f32"
+            if fp64 and seis.shape[0] > 64:
+                out["rec_every_f64"] = np.array(4)
+                seis = seis[::4]
+            out[f"seis_{tag}"] = seis
+            for k, v in summ.items():
+                out[f"{k}_{tag}"] = v
+        np.savez_compressed(os.path.join(HERE, f"ref_{name}.npz"), **out)
+        print(name, {k: v.shape for k, v in out.items()})
+
+
 def main():
     import oracle
 
+    if "--full" in sys.argv:
+        rest = [a for a in sys.argv[1:] if a != "--full"]
+        main_full(rest or None)
+        return
     if oracle.reference_binary(False) is None:
         raise SystemExit("build the reference program first: python oracle/make_ref.py")
     for name, (p, cp, cs, rho) in cases().items():

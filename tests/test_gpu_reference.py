@@ -6,6 +6,8 @@
 - Full-size accuracy of the production FP32 path against the FP64 build of
   the same kernels: every seismogram within 1e-4 relative L2 (the target),
   with the final wavefield's error reported.
+- The two benchmark workloads at full size against the reference program's
+  own FP32 and FP64 runs (tests/golden/ref_*_full.npz).
 - Symmetry of a centred source in a homogeneous cube (full-size indexing).
 """
 import glob
@@ -22,7 +24,9 @@ sys.path.insert(0, os.path.join(HERE, "golden"))
 import make_golden  # noqa: E402
 
 pytestmark = pytest.mark.gpu
-GOLD = sorted(glob.glob(os.path.join(HERE, "golden", "ref_*.npz")))
+# the small cases; the full-size workloads (ref_*_full.npz) are tested apart
+GOLD = sorted(g for g in glob.glob(os.path.join(HERE, "golden", "ref_*.npz")) if not g.endswith("_full.npz"))
+FULL = {os.path.basename(g)[4:-4]: g for g in glob.glob(os.path.join(HERE, "golden", "ref_*_full.npz"))}
 CASES = make_golden.cases()
 
 
@@ -98,6 +102,45 @@ def test_anticline_256_fp32_vs_fp64(built):
           f"final wavefield {max(wave):.2e}")
     assert max(per_rec) <= 1e-4 and whole <= 1e-4
     assert max(wave) <= 1e-3
+
+
+@pytest.mark.parametrize("name", ["homogeneous_101_full", "anticline_256_full"])
+def test_full_size_against_reference_program(built, name):
+    """The benchmark workloads at full size (101^3 x 1000 steps; the 256^3
+    anticline shot x 2000 steps with its 201 receivers) against the
+    reference CPU program's own float32 and float64 runs on the same inputs
+    (tests/golden/ref_<name>.npz).  FP64 GPU within 1e-9 of the FP64
+    program; FP32 GPU within 1e-4 of the FP64 program on every seismogram
+    (the accuracy target) and within 1e-4 of the FP32 program overall."""
+    path = FULL.get(name)
+    if path is None:
+        pytest.skip(f"ref_{name}.npz not generated")
+    p, cp, cs, rho = make_golden.full_cases()[name]
+    g = np.load(path)
+    assert str(g["params"]) == make_golden.params_json(p), "case definition drifted from the fixture"
+    every = int(g["rec_every_f64"]) if "rec_every_f64" in g else 1
+    ref32, ref64 = g["seis_f32"].astype(np.float64), g["seis_f64"]
+    s32, f32 = run(p, cp, cs, rho)
+    s64, f64 = run(p.with_(precision=1), cp, cs, rho)
+    s32 = s32.astype(np.float64)
+    res = {}
+    res["fp64_gpu_vs_fp64_ref"] = seismogram_errors(s64[::every], ref64)
+    res["fp32_gpu_vs_fp64_ref"] = seismogram_errors(s32[::every], ref64)
+    res["fp32_ref_vs_fp64_ref"] = seismogram_errors(ref32[::every], ref64)
+    res["fp32_gpu_vs_fp32_ref"] = seismogram_errors(s32, ref32)
+    for k, (per, whole) in res.items():
+        print(f"{name} {k}: worst seismogram rel L2 {max(per):.2e}, all receivers {whole:.2e}")
+    summ32, summ64 = make_golden.summarize(p, f32), make_golden.summarize(p, f64)
+    wave32 = max(rel_l2(summ32[k][c], g[f"{k}_f64"][c]) for k in ("slice_xy", "slice_yz") for c in range(9)
+                 if np.any(g[f"{k}_f64"][c]))
+    wave64 = max(rel_l2(summ64[k][c], g[f"{k}_f64"][c]) for k in ("slice_xy", "slice_yz") for c in range(9)
+                 if np.any(g[f"{k}_f64"][c]))
+    print(f"{name} final-field slices vs FP64 reference: FP32 GPU {wave32:.2e}, FP64 GPU {wave64:.2e}")
+    assert max(res["fp64_gpu_vs_fp64_ref"][0]) <= 1e-9
+    assert wave64 <= 1e-9
+    assert max(res["fp32_gpu_vs_fp64_ref"][0]) <= 1e-4
+    assert res["fp32_gpu_vs_fp32_ref"][1] <= 1e-4
+    assert wave32 <= 1e-3
 
 
 def test_anticline_256_linear_in_the_source_amplitude(built):

@@ -18,7 +18,9 @@ sys.path.insert(0, os.path.join(HERE, "golden"))
 
 import make_golden  # noqa: E402
 
-GOLD = sorted(glob.glob(os.path.join(HERE, "golden", "ref_*.npz")))
+# the small cases; the full-size workloads (ref_*_full.npz) are tested apart
+GOLD = sorted(g for g in glob.glob(os.path.join(HERE, "golden", "ref_*.npz")) if not g.endswith("_full.npz"))
+FULL = {os.path.basename(g)[4:-4]: g for g in glob.glob(os.path.join(HERE, "golden", "ref_*_full.npz"))}
 CASES = make_golden.cases()
 
 
@@ -45,6 +47,26 @@ def test_oracle_reproduces_reference_goldens(path):
         assert np.array_equal(s["slice_yz"], g[f"slice_yz_{tag}"]), (name, tag)
         assert np.array_equal(s["sum"], g[f"sum_{tag}"]), (name, tag)
         assert np.array_equal(s["sumsq"], g[f"sumsq_{tag}"]), (name, tag)
+
+
+def test_oracle_reproduces_reference_on_the_full_101_cube():
+    """The 101^3 homogeneous cube for all of its 1000 steps: the restatement
+    equals the reference program's float32 and float64 runs bit for bit
+    (about a minute of CPU)."""
+    import oracle
+
+    path = FULL.get("homogeneous_101_full")
+    if path is None:
+        pytest.skip("ref_homogeneous_101_full.npz not generated")
+    p, cp, cs, rho = make_golden.full_cases()["homogeneous_101_full"]
+    g = np.load(path)
+    assert str(g["params"]) == make_golden.params_json(p), "case definition drifted from the fixture"
+    for tag, fp64 in (("f32", False), ("f64", True)):
+        seis, fields = oracle.run(p, cp, cs, rho, fp64=fp64)
+        assert np.array_equal(seis, g[f"seis_{tag}"]), (tag, "seismograms")
+        s = make_golden.summarize(p, fields)
+        for key in ("slice_xy", "slice_yz", "sum", "sumsq"):
+            assert np.array_equal(s[key], g[f"{key}_{tag}"]), (tag, key)
 
 
 def _random_case(seed):
