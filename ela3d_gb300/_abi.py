@@ -47,6 +47,9 @@ SIGNATURES = [
     ("ela3d_set_kernel_timing", _c.c_int, [_P, _c.c_int32]),
     ("ela3d_get_kernel_timing", _c.c_int, [_P, _c.POINTER(_c.c_double), _c.POINTER(_c.c_double),
                                            _c.POINTER(_c.c_int64), _c.POINTER(_c.c_int64)]),
+    ("ela3d_get_flow_timing", _c.c_int, [_P, _c.POINTER(_c.c_double), _c.POINTER(_c.c_int64),
+                                         _c.POINTER(_c.c_int64)]),
+    ("ela3d_flow_schedule_build", _c.c_int, [_c.c_int32] * 9 + [_c.POINTER(_c.c_int32), _P]),
     ("ela3d_plan_destroy", _c.c_int, [_P]),
     ("ela3d_plan_inject_timeout", _c.c_int, [_P, _c.c_int32]),
     ("ela3d_plan_poison_padding", _c.c_int, [_P, _c.c_double]),
@@ -102,14 +105,32 @@ class VariantInfo(ctypes.Structure):
 class Tuning(ctypes.Structure):
     """ela3d_tuning; -1 / 0 fields leave the choice to the library."""
     _fields_ = [("variant", ctypes.c_int32), ("schedule", ctypes.c_int32), ("chunk", ctypes.c_int32),
-                ("blocks_per_sm", ctypes.c_int32), ("prefetch", ctypes.c_int32)]
+                ("blocks_per_sm", ctypes.c_int32), ("prefetch", ctypes.c_int32), ("lag", ctypes.c_int32)]
 
     def __init__(self, variant: int = -1, schedule: int = -1, chunk: int = 0, blocks_per_sm: int = -1,
-                 prefetch: int = -1):
-        super().__init__(variant, schedule, chunk, blocks_per_sm, prefetch)
+                 prefetch: int = -1, lag: int = -1):
+        super().__init__(variant, schedule, chunk, blocks_per_sm, prefetch, lag)
 
     def as_dict(self) -> dict:
-        return {"variant": self.variant, "schedule": self.schedule, "chunk": self.chunk, "prefetch": self.prefetch}
+        return {"variant": self.variant, "schedule": self.schedule, "chunk": self.chunk, "prefetch": self.prefetch,
+                "lag": self.lag}
+
+
+# the dataflow kernel (many steps per cooperative launch): steps in
+# sequence, or overlapping
+SCHEDULE_FLOW, SCHEDULE_FLOW_OVERLAP = 3, 4
+
+
+def flow_schedule(nx, ny, nz, tile_x, tile_y, chunk, gap, overlap, nsteps):
+    """The dataflow work list of one shot (ela3d_flow_schedule_build):
+    items [n, 6] of (kind, step, chunk, tile, k0, k1) in launch order."""
+    lib = load_library()
+    n = ctypes.c_int32()
+    args = (nx, ny, nz, tile_x, tile_y, chunk, gap, 1 if overlap else 0, nsteps, ctypes.byref(n))
+    _check(lib.ela3d_flow_schedule_build(*args, None), "ela3d_flow_schedule_build")
+    items = np.zeros((n.value, 6), np.int32)
+    _check(lib.ela3d_flow_schedule_build(*args, items.ctypes.data), "ela3d_flow_schedule_build")
+    return items
 
 
 def variants() -> list[VariantInfo]:
@@ -220,7 +241,7 @@ class Plan:
 
     def __init__(self, params: ShotParams, cp: np.ndarray, cs: np.ndarray, rho: np.ndarray,
                  variant: int = -1, schedule: int = -1, chunk: int = 0, blocks_per_sm: int = -1,
-                 prefetch: int = -1):
+                 prefetch: int = -1, lag: int = -1):
         lib = load_library()
         self._lib = lib
         self.params = params
@@ -230,14 +251,14 @@ class Plan:
             raise ValueError("model arrays must hold nx*ny*nz float32 values")
         c, rec = params.to_c()
         h = ctypes.c_void_p()
-        t = Tuning(variant, schedule, chunk, blocks_per_sm, prefetch)
+        t = Tuning(variant, schedule, chunk, blocks_per_sm, prefetch, lag)
         _check(lib.ela3d_plan_create_tuned(ctypes.byref(c), _ptr(models[0]), _ptr(models[1]), _ptr(models[2]),
                                            ctypes.byref(t), ctypes.byref(h)), "ela3d_plan_create")
         self._h = h
 
     @classmethod
     def from_model(cls, params: ShotParams, spec: dict, variant: int = -1, schedule: int = -1,
-                   chunk: int = 0, prefetch: int = -1) -> "Plan":
+                   chunk: int = 0, prefetch: int = -1, lag: int = -1) -> "Plan":
         """A plan whose model is generated on the device (ela3d_plan_create_model)."""
         self = cls.__new__(cls)
         lib = load_library()
@@ -245,7 +266,7 @@ class Plan:
         self.params = params
         c, rec = params.to_c()
         m = ModelSpec.from_dict(spec)
-        t = Tuning(variant, schedule, chunk, -1, prefetch)
+        t = Tuning(variant, schedule, chunk, -1, prefetch, lag)
         h = ctypes.c_void_p()
         _check(lib.ela3d_plan_create_model(ctypes.byref(c), ctypes.byref(m), ctypes.byref(t), ctypes.byref(h)),
                "ela3d_plan_create_model")
@@ -321,6 +342,14 @@ class Plan:
     def set_kernel_timing(self, on: bool) -> None:
         _check(self._lib.ela3d_set_kernel_timing(self._h, 1 if on else 0), "ela3d_set_kernel_timing")
 
+    def flow_timing(self) -> tuple[float, int, int]:
+        """(ms, launches, steps) of the dataflow launches timed since
+        set_kernel_timing(True) (ela3d_get_flow_timing)."""
+        ms, nl, ns = ctypes.c_double(), ctypes.c_int64(), ctypes.c_int64()
+        _check(self._lib.ela3d_get_flow_timing(self._h, ctypes.byref(ms), ctypes.byref(nl), ctypes.byref(ns)),
+               "ela3d_get_flow_timing")
+        return ms.value, nl.value, ns.value
+
     def kernel_timing(self) -> tuple[float, float, int, int]:
         a, b = ctypes.c_double(), ctypes.c_double()
         na, nb = ctypes.c_int64(), ctypes.c_int64()
@@ -380,7 +409,7 @@ class Batch:
     shots stores that model once on the device."""
 
     def __init__(self, shots, variant: int = -1, schedule: int = -1, chunk: int = 0, blocks_per_sm: int = -1,
-                 prefetch: int = -1):
+                 prefetch: int = -1, lag: int = -1):
         lib = load_library()
         self._lib = lib
         self.params = [s[0] for s in shots]
@@ -402,7 +431,7 @@ class Batch:
                     seen[id(arr)] = m
                     keep.append(m)
                 ptrs[key][i] = m.ctypes.data
-        t = Tuning(variant, schedule, chunk, blocks_per_sm, prefetch)
+        t = Tuning(variant, schedule, chunk, blocks_per_sm, prefetch, lag)
         h = ctypes.c_void_p()
         _check(lib.ela3d_batch_create(n, structs, ptrs["cp"], ptrs["cs"], ptrs["rho"], ctypes.byref(t),
                                       ctypes.byref(h)), "ela3d_batch_create")
@@ -483,7 +512,7 @@ class Server:
 
     def __init__(self, hbm_budget_bytes: int = 0, max_active: int = 0, steps_per_round: int = 50,
                  precision: int = 0, variant: int = -1, schedule: int = -1, chunk: int = 0, prefetch: int = -1,
-                 fill_cells: int = 0):
+                 fill_cells: int = 0, lag: int = -1):
         lib = load_library()
         self._lib = lib
         cfg = ServerConfig()
@@ -493,7 +522,7 @@ class Server:
         cfg.steps_per_round = steps_per_round
         cfg.precision = precision
         cfg.fill_cells = fill_cells
-        cfg.tune = Tuning(variant, schedule, chunk, -1, prefetch)
+        cfg.tune = Tuning(variant, schedule, chunk, -1, prefetch, lag)
         h = ctypes.c_void_p()
         _check(lib.ela3d_server_create(ctypes.byref(cfg), ctypes.byref(h)), "ela3d_server_create")
         self._h = h

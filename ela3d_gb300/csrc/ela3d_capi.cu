@@ -35,8 +35,13 @@ ela3d_status ela3d::validate_tuning(const ela3d_tuning *t, int32_t precision) {
     set_last_error("kernel variant of the other precision");
     return ELA3D_ERR_INVALID_ARG;
   }
-  if (t->schedule < -1 || t->schedule > 2 || t->chunk < 0 || t->blocks_per_sm < -1 || t->prefetch < -1) {
+  if (t->schedule < -1 || t->schedule > kScheduleFlowOverlap || t->chunk < 0 || t->blocks_per_sm < -1 ||
+      t->prefetch < -1 || t->lag < -1) {
     set_last_error("tuning field out of range");
+    return ELA3D_ERR_INVALID_ARG;
+  }
+  if (t->schedule >= kScheduleFlow && t->chunk == 1) {
+    set_last_error("the dataflow schedule needs z-chunks of at least 2 planes");
     return ELA3D_ERR_INVALID_ARG;
   }
   return ELA3D_OK;
@@ -152,6 +157,7 @@ static TuneChoice resolve_tuning(const std::vector<ela3d_params> &ps, const floa
   if (t->chunk > 0) c.chunk = t->chunk;
   if (t->blocks_per_sm >= 0) c.blocks_per_sm = t->blocks_per_sm;
   if (t->prefetch >= 0) c.prefetch = t->prefetch & (CTL_PF_X | CTL_PF_YZ);
+  if (t->lag >= 0) c.lag = t->lag;
   return c;
 }
 
@@ -357,6 +363,11 @@ ela3d_status ela3d_get_kernel_timing(ela3d_plan *plan, double *stress_ms, double
   return plan->eng->timing(stress_ms, velocity_ms, stress_launches, velocity_launches);
 }
 
+ela3d_status ela3d_get_flow_timing(ela3d_plan *plan, double *ms, int64_t *launches, int64_t *steps) {
+  if (!plan) return ELA3D_ERR_INVALID_ARG;
+  return plan->eng->flow_timing(ms, launches, steps);
+}
+
 ela3d_status ela3d_plan_check_guards(ela3d_plan *plan) {
   if (!plan) return ELA3D_ERR_INVALID_ARG;
   return plan->eng->check_guards();
@@ -388,6 +399,31 @@ ela3d_status ela3d_slab_extent(const double *a_full, const double *a_half, int32
   slab_extent(a_full, a_half, n, &l, &h);
   *lo = l;
   *hi = h;
+  return ELA3D_OK;
+}
+
+ela3d_status ela3d_flow_schedule_build(int32_t nx, int32_t ny, int32_t nz, int32_t tile_x, int32_t tile_y,
+                                       int32_t chunk, int32_t gap, int32_t overlap, int32_t nsteps,
+                                       int32_t *nitems, int32_t *items) {
+  if (nx < 1 || ny < 1 || nz < 1 || !nitems) return ELA3D_ERR_INVALID_ARG;
+  std::vector<FlowItem> it;
+  std::vector<int> off, nch;
+  int nflags = 0;
+  std::string why;
+  if (!build_flow_schedule({FlowShape{nx, ny, nz, 0}}, tile_x, tile_y, chunk, gap, overlap != 0, nsteps, &it, &off,
+                           &nch, &nflags, &why)) {
+    set_last_error(why);
+    return ELA3D_ERR_INVALID_ARG;
+  }
+  if (items) {
+    if (*nitems < (int32_t)it.size()) return ELA3D_ERR_INVALID_ARG;
+    for (size_t q = 0; q < it.size(); ++q) {
+      int32_t *o = items + 6 * q;
+      o[0] = it[q].kind; o[1] = it[q].step; o[2] = it[q].chunk;
+      o[3] = it[q].it.tile; o[4] = it[q].it.k0; o[5] = it[q].it.k1;
+    }
+  }
+  *nitems = (int32_t)it.size();
   return ELA3D_OK;
 }
 

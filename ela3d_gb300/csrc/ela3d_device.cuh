@@ -82,6 +82,8 @@ struct ShotDesc {
   T *src_trace;              // [3][nstep + 1]: the source cell's injected components
                              // (sxx syy szz, or vx vy vz for a force) after step it's
                              // injection at index it; index 0 stays 0
+  int *flow_flags;           // dataflow kernel: completion counters [2][flow_chunks][tiles]
+  int flow_chunks;           // z-chunks of the dataflow schedule (0: none)
 };
 
 // Tensor maps of one shot.  Box shapes (TX, TY = tile; H = 16 bytes of T):
@@ -100,6 +102,14 @@ struct ShotMaps {
 // One work item: a z-run [k0, k1) of one x-y tile of one shot.
 struct Item {
   int shot, tile, k0, k1;
+};
+
+// A work item of the dataflow kernel: the stress (kind 0) or velocity
+// (kind 1) half-step of one item at step `step` of the launch, in z-chunk
+// `chunk` of the shot's dataflow schedule.
+struct FlowItem {
+  Item it;
+  int kind, step, chunk, pad;
 };
 
 // ---------------------------------------------------------------- PTX ----

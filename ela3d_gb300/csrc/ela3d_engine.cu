@@ -182,6 +182,115 @@ void build_schedule(const std::vector<ShotShape> &shots, int tx, int ty, int kin
   }
 }
 
+bool build_flow_schedule(const std::vector<FlowShape> &shots, int tx, int ty, int chunk, int gap, bool overlap,
+                         int nsteps, std::vector<FlowItem> *items, std::vector<int> *flag_off,
+                         std::vector<int> *nchunks, int *nflags, std::string *why) {
+  items->clear();
+  flag_off->clear();
+  nchunks->clear();
+  *nflags = 0;
+  if (chunk < 2 || gap < 1 || nsteps < 1 || tx < 1 || ty < 1) {
+    *why = "dataflow schedule: chunk >= 2, gap >= 1, nsteps >= 1";
+    return false;
+  }
+  // Keys approximate list positions (two per stress item of one step in
+  // natural order, leaving room for the velocity items between them): a
+  // stress item of step 0 sits at its natural place, every other item `gap`
+  // after the last item it waits for (a stress item of a later step also
+  // no earlier than its natural place, plus the whole steps before it
+  // unless steps may overlap).
+  struct Keyed { long long key; int shot, step, kind, chunk, tile; FlowItem fi; };
+  std::vector<Keyed> all;
+  std::vector<int> txs_of, tys_of;
+  for (int s = 0; s < (int)shots.size(); ++s) {
+    const FlowShape &sh = shots[s];
+    const int txs = (sh.nx + tx - 1) / tx, tys = (sh.ny + ty - 1) / ty, nt = txs * tys;
+    const int J = (sh.nz + chunk - 1) / chunk;
+    txs_of.push_back(txs);
+    tys_of.push_back(tys);
+    flag_off->push_back(*nflags);
+    nchunks->push_back(J);
+    *nflags += 2 * J * nt;
+    std::vector<long long> ks((size_t)J * nt), kv((size_t)J * nt), ks_prev, kv_prev;
+    auto idx = [&](int j, int t) { return (size_t)j * nt + t; };
+    // the items one item waits for (chunks c0/c1 of the other kind, on the
+    // tile and its four neighbours): the largest key among them
+    auto last_dep = [&](const std::vector<long long> &k, int c0, int c1, int t) {
+      const int x = t % txs, y = t / txs;
+      const int nb[5][2] = {{x, y}, {x - 1, y}, {x + 1, y}, {x, y - 1}, {x, y + 1}};
+      long long m = -1;
+      for (auto &b : nb) {
+        if (b[0] < 0 || b[0] >= txs || b[1] < 0 || b[1] >= tys) continue;
+        for (int c : {c0, c1})
+          if (c >= 0 && c < J) m = std::max(m, k[idx(c, b[1] * txs + b[0])]);
+      }
+      return m;
+    };
+    long long step_base = 0;   // without overlap: past every key of the previous step
+    for (int r = 0; r < nsteps; ++r) {
+      for (int j = 0; j < J; ++j)
+        for (int t = 0; t < nt; ++t) {
+          long long key = 2ll * ((long long)j * nt + t) + step_base;
+          if (r > 0) key = std::max(key, last_dep(kv_prev, j, j + 1, t) + gap);
+          ks[idx(j, t)] = key;
+          const int k0 = j * chunk, k1 = std::min((j + 1) * chunk, sh.nz);
+          all.push_back({key, s, r, 0, j, t, FlowItem{{sh.id, t, k0, k1}, 0, r, j, 0}});
+        }
+      for (int j = 0; j < J; ++j)
+        for (int t = 0; t < nt; ++t) {
+          const long long key = last_dep(ks, j - 1, j, t) + gap;
+          kv[idx(j, t)] = key;
+          const int k0 = std::max(j * chunk - 1, 0), k1 = (j == J - 1) ? sh.nz : (j + 1) * chunk - 1;
+          all.push_back({key, s, r, 1, j, t, FlowItem{{sh.id, t, k0, k1}, 1, r, j, 0}});
+        }
+      ks_prev = ks;
+      kv_prev = kv;
+      if (!overlap) step_base = *std::max_element(kv.begin(), kv.end()) + 1;
+    }
+  }
+  std::stable_sort(all.begin(), all.end(), [](const Keyed &a, const Keyed &b) {
+    if (a.key != b.key) return a.key < b.key;
+    if (a.step != b.step) return a.step < b.step;
+    if (a.kind != b.kind) return a.kind < b.kind;
+    if (a.shot != b.shot) return a.shot < b.shot;
+    if (a.chunk != b.chunk) return a.chunk < b.chunk;
+    return a.tile < b.tile;
+  });
+  // check: every item comes after every item it waits for
+  std::vector<std::vector<int>> pos(shots.size());
+  for (size_t s = 0; s < shots.size(); ++s)
+    pos[s].assign((size_t)nsteps * 2 * (*nchunks)[s] * txs_of[s] * tys_of[s], -1);
+  auto at = [&](int s, int r, int kind, int j, int t) -> int & {
+    const int J = (*nchunks)[s], nt = txs_of[s] * tys_of[s];
+    return pos[s][(((size_t)r * 2 + kind) * J + j) * nt + t];
+  };
+  for (size_t q = 0; q < all.size(); ++q) at(all[q].shot, all[q].step, all[q].kind, all[q].chunk, all[q].tile) = (int)q;
+  for (size_t q = 0; q < all.size(); ++q) {
+    const int s = all[q].shot;
+    const FlowItem &f = all[q].fi;
+    const int txs = txs_of[s], tys = tys_of[s], J = (*nchunks)[s];
+    const int tx0 = f.it.tile % txs, ty0 = f.it.tile / txs;
+    const int r = f.kind == 0 ? f.step - 1 : f.step;   // step of the items waited for
+    if (r < 0) continue;                               // before the launch: done
+    const int c0 = f.chunk, c1 = f.kind == 0 ? (f.chunk + 1 < J ? f.chunk + 1 : -1) : f.chunk - 1;
+    const int nb[5][2] = {{tx0, ty0}, {tx0 - 1, ty0}, {tx0 + 1, ty0}, {tx0, ty0 - 1}, {tx0, ty0 + 1}};
+    for (auto &b : nb) {
+      if (b[0] < 0 || b[0] >= txs || b[1] < 0 || b[1] >= tys) continue;
+      for (int c : {c0, c1}) {
+        if (c < 0) continue;
+        const int d = at(s, r, 1 - f.kind, c, b[1] * txs + b[0]);
+        if (d < 0 || d >= (int)q) {
+          *why = "dataflow schedule: an item does not follow the items it waits for";
+          return false;
+        }
+      }
+    }
+  }
+  items->reserve(all.size());
+  for (auto &k : all) items->push_back(k.fi);
+  return true;
+}
+
 TuneChoice default_choice(int fp64, int nx, int ny, int nz) {
   int n = 0;
   const Variant *v = variants(&n);
@@ -682,11 +791,10 @@ class Engine final : public EngineBase {
     }
     CK(cudaFuncSetAttribute(var_->stress, cudaFuncAttributeMaxDynamicSharedMemorySize, var_->stress_smem));
     CK(cudaFuncSetAttribute(var_->velocity, cudaFuncAttributeMaxDynamicSharedMemorySize, var_->vel_smem));
-    int occ_s = 0, occ_v = 0;
-    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_s, var_->stress, var_->threads, var_->stress_smem));
-    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_v, var_->velocity, var_->threads, var_->vel_smem));
-    per_sm_ = std::max(1, std::min(occ_s, occ_v));
-    if (c.blocks_per_sm > 0) per_sm_ = std::min(per_sm_, c.blocks_per_sm);
+    if (var_->flow)
+      CK(cudaFuncSetAttribute(var_->flow, cudaFuncAttributeMaxDynamicSharedMemorySize, var_->flow_smem));
+    ela3d_status ost = occupancy(c);
+    if (ost != ELA3D_OK) return ost;
     if (!shots_.empty()) {
       ela3d_status st = upload_tables();
       if (st != ELA3D_OK) return st;
@@ -702,14 +810,37 @@ class Engine final : public EngineBase {
     if (c.variant < 0 || c.variant >= nv || var_ != &vs[c.variant]) BAD("retune keeps the kernel variant");
     choice_ = c;
     prefetch_ = prefetch_env_ >= 0 ? prefetch_env_ : (c.prefetch & (CTL_PF_X | CTL_PF_YZ));
+    ela3d_status ost = occupancy(c);
+    if (ost != ELA3D_OK) return ost;
+    sched_valid_ = false;
+    sched_key_.clear();
+    return rebuild_schedule();
+  }
+
+  // Resident blocks per SM of the half-step kernels and of the dataflow
+  // kernel (its launch is cooperative: every block must be resident).
+  ela3d_status occupancy(const TuneChoice &c) {
     int occ_s = 0, occ_v = 0;
     CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_s, var_->stress, var_->threads, var_->stress_smem));
     CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_v, var_->velocity, var_->threads, var_->vel_smem));
     per_sm_ = std::max(1, std::min(occ_s, occ_v));
     if (c.blocks_per_sm > 0) per_sm_ = std::min(per_sm_, c.blocks_per_sm);
-    sched_valid_ = false;
-    sched_key_.clear();
-    return rebuild_schedule();
+    per_sm_flow_ = 0;
+    if (var_->flow) {
+      int occ_f = 0;
+      CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ_f, var_->flow, var_->threads, var_->flow_smem));
+      per_sm_flow_ = occ_f;
+      if (c.blocks_per_sm > 0) per_sm_flow_ = std::min(per_sm_flow_, c.blocks_per_sm);
+    }
+    return ELA3D_OK;
+  }
+
+  // The dataflow kernel runs when the schedule asks for it and it can: a
+  // compiled dataflow kernel, resident blocks, and no explosive source (its
+  // injection into the stresses runs as a kernel between the steps).
+  bool flow_on() const {
+    return (choice_.kind == kScheduleFlow || choice_.kind == kScheduleFlowOverlap) && var_ && var_->flow &&
+           per_sm_flow_ > 0 && !any_explosive_;
   }
 
   // Retire shots once they reach their nstep (batches with uneven lengths):
@@ -767,6 +898,17 @@ class Engine final : public EngineBase {
       nsteps -= seg;
       if (nblocks_ == 0) {
         tick_ += seg;
+        continue;
+      }
+      if (flow_on() && flow_steps_ > 0) {
+        while (seg > 0) {
+          const int k = std::min(seg, flow_steps_);
+          ela3d_status st = launch_flow(tick_ + 1, k);
+          if (st != ELA3D_OK) return st;
+          tick_ += k;
+          seg -= k;
+          steps_on_schedule_ += k;
+        }
         continue;
       }
       // a composition's first kGraphSteps steps run as direct launches; the
@@ -877,7 +1019,9 @@ class Engine final : public EngineBase {
     }
     std::vector<Item> items;
     std::vector<int2> ranges;
-    build_schedule(shapes, var_->tx, var_->ty, choice_.kind, choice_.chunk, per_sm_ * num_sms_, &items, &ranges);
+    const int kind = choice_.kind >= kScheduleFlow ? 1 : choice_.kind;
+    build_schedule(shapes, var_->tx, var_->ty, kind, std::max(choice_.chunk, 1), per_sm_ * num_sms_, &items,
+                   &ranges);
     if (items.empty()) BAD("empty schedule");
     for (const Item &it : items)
       if (it.k1 <= it.k0) BAD("internal: empty work item");
@@ -898,6 +1042,85 @@ class Engine final : public EngineBase {
     CK(cudaMemcpy(d_ranges_, ranges.data(), ranges.size() * sizeof(int2), cudaMemcpyHostToDevice));
     nblocks_ = (int)ranges.size();
     nitems_ = (int)items.size();
+    flow_items_ = 0;
+    flow_steps_ = 0;
+    if (flow_on()) return rebuild_flow(key);
+    return ELA3D_OK;
+  }
+
+  // The dataflow list of the active shots for up to kFlowSteps steps per
+  // launch (fewer when the list would pass kFlowMaxItems items), their
+  // completion counters, and the descriptors that point at them.
+  ela3d_status rebuild_flow(const std::vector<int> &active) {
+    std::vector<FlowShape> shapes;
+    long long per_step = 0;
+    const int C = std::max(choice_.chunk, 2);
+    for (int q : active) {
+      const ShotDesc<T> &d = shots_[q]->d;
+      shapes.push_back({d.nx, d.ny, d.nz, q});
+      const long long nt = (long long)((d.nx + var_->tx - 1) / var_->tx) * ((d.ny + var_->ty - 1) / var_->ty);
+      per_step += 2 * nt * ((d.nz + C - 1) / C);
+    }
+    const int K = (int)std::max<long long>(1, std::min<long long>(kFlowSteps, kFlowMaxItems / std::max(1ll, per_step)));
+    std::vector<FlowItem> items;
+    std::vector<int> off, nch;
+    int nflags = 0;
+    std::string why;
+    // gap: by default about one round of the grid, so an item is claimed
+    // when the items it waits for have finished while their results are
+    // still in L2
+    const int gap = choice_.lag > 0 ? choice_.lag : std::max(1, per_sm_flow_ * num_sms_);
+    if (!build_flow_schedule(shapes, var_->tx, var_->ty, C, gap, choice_.kind == kScheduleFlowOverlap, K, &items,
+                             &off, &nch, &nflags, &why))
+      BAD(why);
+    CK(cudaStreamSynchronize(stream_));
+    if (items.size() > flow_cap_) {
+      if (d_flow_) CK(cudaFree(d_flow_));
+      d_flow_ = nullptr;
+      flow_cap_ = 0;
+      CK(cudaMalloc(&d_flow_, items.size() * sizeof(FlowItem)));
+      flow_cap_ = items.size();
+    }
+    if ((size_t)nflags > flags_cap_) {
+      if (d_flags_) CK(cudaFree(d_flags_));
+      d_flags_ = nullptr;
+      flags_cap_ = 0;
+      CK(cudaMalloc(&d_flags_, (size_t)nflags * sizeof(int)));
+      flags_cap_ = (size_t)nflags;
+    }
+    CK(cudaMemcpy(d_flow_, items.data(), items.size() * sizeof(FlowItem), cudaMemcpyHostToDevice));
+    for (size_t a = 0; a < active.size(); ++a) {
+      ShotDesc<T> &d = shots_[active[a]]->d;
+      d.flow_flags = d_flags_ + off[a];
+      d.flow_chunks = nch[a];
+    }
+    ela3d_status st = upload_tables();
+    if (st != ELA3D_OK) return st;
+    flow_items_ = (int)items.size();
+    flow_steps_ = K;
+    flags_used_ = (size_t)nflags;
+    return ELA3D_OK;
+  }
+
+  // One launch of the dataflow kernel: steps tick .. tick + nsteps - 1.
+  ela3d_status launch_flow(int tick, int nsteps) {
+    int ctl = (inject_ > 0 ? CTL_WITHHOLD_LOADS : 0) | prefetch_;
+    inject_ = std::max(0, inject_ - nsteps);
+    const int *dtick = nullptr;
+    void *args[] = {&d_desc_, &d_maps_, &d_flow_, &flow_items_, &nsteps, &tick, &dtick, &d_err_, &ctl};
+    CK(cudaMemsetAsync(d_flags_, 0, flags_used_ * sizeof(int), stream_));
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (timing_) {
+      e0 = event(); e1 = event();
+      CK(cudaEventRecord(e0, stream_));
+    }
+    const int grid = std::min(per_sm_flow_ * num_sms_, std::max(1, flow_items_));
+    CK(cudaLaunchCooperativeKernel(var_->flow, dim3(grid), dim3(var_->threads), args, var_->flow_smem, stream_));
+    if (timing_) {
+      CK(cudaEventRecord(e1, stream_));
+      pending_.push_back({e0, e1, nullptr, nsteps});
+    }
+    launches_ += 1;
     return ELA3D_OK;
   }
 
@@ -1195,6 +1418,15 @@ class Engine final : public EngineBase {
     return ELA3D_OK;
   }
 
+  ela3d_status flow_timing(double *ms, int64_t *launches, int64_t *steps) override {
+    CK(cudaStreamSynchronize(stream_));
+    collect_timing();
+    if (ms) *ms = t_flow_;
+    if (launches) *launches = n_flow_;
+    if (steps) *steps = steps_flow_;
+    return ELA3D_OK;
+  }
+
   ela3d_status timing(double *s_ms, double *v_ms, int64_t *ns, int64_t *nv) override {
     CK(cudaStreamSynchronize(stream_));
     collect_timing();
@@ -1253,6 +1485,12 @@ class Engine final : public EngineBase {
   void collect_timing() {
     for (auto &t : pending_) {
       float a = 0.f, b = 0.f;
+      if (!t.e2) {
+        if (cudaEventElapsedTime(&a, t.e0, t.e1) == cudaSuccess) { t_flow_ += a; ++n_flow_; steps_flow_ += t.flow_steps; }
+        free_events_.push_back(t.e0);
+        free_events_.push_back(t.e1);
+        continue;
+      }
       if (cudaEventElapsedTime(&a, t.e0, t.e1) == cudaSuccess) { t_stress_ += a; ++n_stress_; }
       if (cudaEventElapsedTime(&b, t.e1, t.e2) == cudaSuccess) { t_vel_ += b; ++n_vel_; }
       free_events_.push_back(t.e0);
@@ -1277,6 +1515,10 @@ class Engine final : public EngineBase {
     if (d_err_) cudaFree(d_err_);
     if (d_energy_) cudaFree(d_energy_);
     if (d_tick_) cudaFree(d_tick_);
+    if (d_flow_) cudaFree(d_flow_);
+    if (d_flags_) cudaFree(d_flags_);
+    d_flow_ = nullptr;
+    d_flags_ = nullptr;
     invalidate_graph();
     if (stream_) cudaStreamDestroy(stream_);
     if (setup_) cudaStreamDestroy(setup_);
@@ -1284,7 +1526,7 @@ class Engine final : public EngineBase {
     d_err_ = nullptr; d_energy_ = nullptr; d_tick_ = nullptr; stream_ = nullptr; setup_ = nullptr;
   }
 
-  struct Ev { cudaEvent_t e0, e1, e2; };
+  struct Ev { cudaEvent_t e0, e1, e2; int flow_steps = 0; };   // e2 null: a dataflow launch
   int device_ = 0, num_sms_ = 1;
   cudaStream_t stream_ = nullptr;
   std::vector<std::unique_ptr<Shot<T>>> shots_;
@@ -1322,6 +1564,15 @@ class Engine final : public EngineBase {
   std::vector<cudaEvent_t> free_events_;
   double t_stress_ = 0.0, t_vel_ = 0.0;
   int64_t n_stress_ = 0, n_vel_ = 0;
+  // dataflow path (schedule kind 3)
+  static constexpr int kFlowSteps = 50;
+  static constexpr long long kFlowMaxItems = 1 << 20;
+  FlowItem *d_flow_ = nullptr;
+  int *d_flags_ = nullptr;
+  size_t flow_cap_ = 0, flags_cap_ = 0, flags_used_ = 0;
+  int flow_items_ = 0, flow_steps_ = 0, per_sm_flow_ = 0;
+  double t_flow_ = 0.0;
+  int64_t n_flow_ = 0, steps_flow_ = 0;
 
 };
 

@@ -47,13 +47,44 @@ struct ShotShape {
 void build_schedule(const std::vector<ShotShape> &shots, int tx, int ty, int kind, int chunk,
                     int max_blocks, std::vector<Item> *items, std::vector<int2> *ranges);
 
+// Dataflow schedules (kinds 3 and 4): the work items of `nsteps` time steps
+// of the shots, for the dataflow kernel.  Each shot's planes are cut into
+// z-chunks of `chunk` (>= 2) planes; stress chunk j covers [j*chunk,
+// (j+1)*chunk), velocity chunk j the same range one plane lower (the first
+// from 0, the last to nz).  Item dependencies: stress of tile t, chunk j,
+// step r waits for velocity of chunks j, j+1 at step r-1 on t and its four
+// neighbours; velocity waits for stress of chunks j-1, j at step r there.
+// Order: a stress item of step 0 at its natural place (chunk by chunk,
+// tile by tile), every other item `gap` places after the last item it
+// waits for -- about one round of the grid, so that it is claimed when
+// those have finished while their results are still in L2; stress items of
+// a later step come after the whole previous step unless `overlap`.  Every
+// item is checked to follow the items it waits for, which is what makes
+// the kernel's waits end.  flag_off[s] is shot s's offset into the
+// completion counters ([2][chunks][tiles] ints each), *nflags their total.
+// False (with *why) on bad arguments or a failed order check.
+struct FlowShape {
+  int nx, ny, nz;
+  int id;   // shot index written into the items
+};
+bool build_flow_schedule(const std::vector<FlowShape> &shots, int tx, int ty, int chunk, int gap, bool overlap,
+                         int nsteps, std::vector<FlowItem> *items, std::vector<int> *flag_off,
+                         std::vector<int> *nchunks, int *nflags, std::string *why);
+
 // A kernel variant, its work schedule and the memory-variable prefetch mode.
 constexpr int kPrefetchDefault = CTL_PF_X | CTL_PF_YZ;
+// Schedule kinds 0-2 launch the two half-step kernels once per step; kinds
+// 3 and 4 run many steps per launch of the dataflow kernel (chunk planes
+// per z-chunk, lag = the gap of build_flow_schedule, 0 = one round of the
+// grid; kind 4 lets consecutive steps overlap).
+constexpr int kScheduleFlow = 3;
+constexpr int kScheduleFlowOverlap = 4;
 struct TuneChoice {
   int variant;     // index into variants()
   int kind, chunk; // schedule
   int blocks_per_sm;  // 0 = occupancy limit
   int prefetch = kPrefetchDefault;  // CTL_PF_* bits
+  int lag = 0;     // kinds 3, 4: gap in items (0 = one round of the grid)
 };
 // Built-in choice when the autotuner's cache has none for the workload.
 TuneChoice default_choice(int fp64, int nx, int ny, int nz);
@@ -110,6 +141,8 @@ class EngineBase {
   virtual int64_t launches() const = 0;
   virtual int64_t device_bytes() const = 0;
   virtual ela3d_status timing(double *s_ms, double *v_ms, int64_t *ns, int64_t *nv) = 0;
+  // Dataflow launches timed since timing was enabled: ms, launches, steps.
+  virtual ela3d_status flow_timing(double *ms, int64_t *launches, int64_t *steps) = 0;
   virtual int nshots() const = 0;
   virtual int steps_done() const = 0;
   virtual cudaStream_t stream() const = 0;

@@ -19,6 +19,8 @@ struct Variant {
   int loads;            // LOAD_TMA or LOAD_CP_ASYNC (how stages are filled)
   const void *stress;   // __global__ entry points
   const void *velocity;
+  const void *flow;     // dataflow kernel (many steps per launch); null if not compiled
+  int flow_smem;
 };
 
 // All compiled variants (ela3d_stencil.cu).

@@ -332,6 +332,7 @@ ela3d_status ela3d_server_config_default(ela3d_server_config *c) {
   c->tune.chunk = 0;
   c->tune.blocks_per_sm = -1;
   c->tune.prefetch = -1;
+  c->tune.lag = -1;
   return ELA3D_OK;
 }
 
@@ -360,6 +361,7 @@ ela3d_status ela3d_server_create(const ela3d_server_config *cfg, ela3d_server **
     if (cfg->tune.chunk > 0) c.chunk = cfg->tune.chunk;
     if (cfg->tune.blocks_per_sm >= 0) c.blocks_per_sm = cfg->tune.blocks_per_sm;
     if (cfg->tune.prefetch >= 0) c.prefetch = cfg->tune.prefetch & (CTL_PF_X | CTL_PF_YZ);
+    if (cfg->tune.lag >= 0) c.lag = cfg->tune.lag;
     s->eng->set_retire(true);
     st = s->eng->finalize(&c);
   }

@@ -22,6 +22,12 @@ static Variant make_variant() {
   v.loads = LOAD;
   v.stress = reinterpret_cast<const void *>(&stress_kernel<T, TX, TY, NS, CPT, MB, LOAD>);
   v.velocity = reinterpret_cast<const void *>(&velocity_kernel<T, TX, TY, NS, CPT, MB, LOAD>);
+  v.flow = nullptr;
+  v.flow_smem = 0;
+  if constexpr (LOAD == LOAD_TMA) {
+    v.flow = reinterpret_cast<const void *>(&flow_kernel<T, TX, TY, NS, CPT, MB>);
+    v.flow_smem = Flow<T, TX, TY, NS, CPT, MB>::SMEM;
+  }
   return v;
 }
 

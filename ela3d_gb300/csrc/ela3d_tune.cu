@@ -34,13 +34,13 @@ void load_locked() {
   if (!f) return;
   FILE *fp = std::fopen(f, "r");
   if (!fp) return;
-  // one line per workload: key variant kind chunk blocks_per_sm prefetch
+  // one line per workload: key variant kind chunk blocks_per_sm prefetch [lag]
   char line[1024], key[512];
   while (std::fgets(line, sizeof line, fp)) {
     TuneChoice c{};
-    if (std::sscanf(line, "%511s %d %d %d %d %d", key, &c.variant, &c.kind, &c.chunk, &c.blocks_per_sm,
-                    &c.prefetch) == 6)
-      g_cache[key] = c;
+    const int got = std::sscanf(line, "%511s %d %d %d %d %d %d", key, &c.variant, &c.kind, &c.chunk,
+                                &c.blocks_per_sm, &c.prefetch, &c.lag);
+    if (got == 6 || got == 7) g_cache[key] = c;
   }
   std::fclose(fp);
 }
@@ -51,8 +51,8 @@ void save_locked() {
   FILE *fp = std::fopen(f, "w");
   if (!fp) return;
   for (auto &kv : g_cache)
-    std::fprintf(fp, "%s %d %d %d %d %d\n", kv.first.c_str(), kv.second.variant, kv.second.kind,
-                 kv.second.chunk, kv.second.blocks_per_sm, kv.second.prefetch);
+    std::fprintf(fp, "%s %d %d %d %d %d %d\n", kv.first.c_str(), kv.second.variant, kv.second.kind,
+                 kv.second.chunk, kv.second.blocks_per_sm, kv.second.prefetch, kv.second.lag);
   std::fclose(fp);
 }
 }  // namespace
@@ -91,8 +91,9 @@ bool tune_lookup(const std::vector<ela3d_params> &ps, TuneChoice *out) {
   int nv = 0;
   const Variant *vs = variants(&nv);
   const bool fp64 = !ps.empty() && ps[0].precision == ELA3D_FP64;
-  if (c.variant < 0 || c.variant >= nv || (vs[c.variant].fp64 != 0) != fp64 || c.kind < 0 || c.kind > 2 ||
-      c.chunk < 0 || c.blocks_per_sm < 0)
+  if (c.variant < 0 || c.variant >= nv || (vs[c.variant].fp64 != 0) != fp64 || c.kind < 0 ||
+      c.kind > kScheduleFlowOverlap || c.chunk < 0 || c.blocks_per_sm < 0 || c.lag < 0 ||
+      (c.kind >= kScheduleFlow && (c.chunk < 2 || !vs[c.variant].flow)))
     return false;
   *out = c;
   out->prefetch &= CTL_PF_X | CTL_PF_YZ;
@@ -196,6 +197,7 @@ extern "C" ela3d_status ela3d_autotune(int32_t nshots, const ela3d_params *param
   best->chunk = bc.chunk;
   best->blocks_per_sm = bc.blocks_per_sm;
   best->prefetch = bc.prefetch;
+  best->lag = bc.lag;
   if (candidates) *candidates = (int32_t)table.size();
   return ELA3D_OK;
 }

@@ -204,6 +204,9 @@ ela3d_status ela3d_set_kernel_timing(ela3d_plan *plan, int32_t enable);
  * and launch counts. */
 ela3d_status ela3d_get_kernel_timing(ela3d_plan *plan, double *stress_ms, double *velocity_ms,
                                      int64_t *stress_launches, int64_t *velocity_launches);
+/* The same for dataflow launches (schedule 3): milliseconds, launches and
+ * the time steps they ran. */
+ela3d_status ela3d_get_flow_timing(ela3d_plan *plan, double *ms, int64_t *launches, int64_t *steps);
 ela3d_status ela3d_plan_destroy(ela3d_plan *plan);
 /* Test hook for the failure path: the kernels of the plan's next `steps`
  * time steps withhold their shared-memory loads, so their bounded device
@@ -248,14 +251,28 @@ typedef struct ela3d_variant_info {
  * ELA3D_ERR_INVALID_ARG, reported before any device work. */
 typedef struct ela3d_tuning {
     int32_t variant;        /* index < ela3d_variant_count(), or -1 */
-    int32_t schedule;       /* 0, 1, 2, or -1 */
-    int32_t chunk;          /* planes per z-chunk for schedules 1 and 2, or 0 */
+    int32_t schedule;       /* 0, 1, 2, 3 or 4 (dataflow, below), or -1 */
+    int32_t chunk;          /* planes per z-chunk for schedules 1-4 (>= 2 for
+                               3 and 4), or 0 */
     int32_t blocks_per_sm;  /* cap on resident blocks per SM, 0 = occupancy limit, -1 */
     int32_t prefetch;       /* prefetch of the C-PML memory variables by the
                                loading warp: bit 1 (2) x slab into L1, bit 2 (4)
                                y and z slabs into L2; -1 = built-in choice
                                (6, or 2 for a shot that fits in L2) */
+    int32_t lag;            /* schedules 3 and 4: places in the work list
+                               between an item and the last item it waits
+                               for; 0 or -1 = one round of the grid */
 } ela3d_tuning;
+/* Schedules 3 and 4 (dataflow): instead of two kernels per time step, one
+ * persistent, cooperative kernel advances up to 50 steps per launch.  Its
+ * work items are the stress or velocity half-step of one (x-y tile,
+ * z-chunk) at one step; each item waits (on device counters) for exactly
+ * the items whose results it reads or overwrites.  The host places every
+ * item `lag` places after the last item it waits for, so it runs soon
+ * after them, while their results are still in L2; schedule 3 keeps the
+ * time steps in sequence, schedule 4 lets a step start where the previous
+ * one is done.  Results are bit-identical to schedules 0-2.  Shots with an
+ * explosive source run the two-kernel path with schedule 1. */
 
 /* Times every compiled variant with the candidate schedules on these shots
  * (`steps` time steps each, after a warm-up) and returns the fastest choice;
@@ -410,6 +427,16 @@ ela3d_status ela3d_slab_extent(const double *a_full, const double *a_half, int32
 /* The work split the kernels use for one grid: items (tile, k0, k1) per
  * block.  With items == NULL only the counts are returned.  No reference
  * counterpart (its launch is a fixed 3-D grid, cudazerocopy.cu:1361-1369). */
+/* Host-only test hook: the dataflow work list (schedules 3 and 4) of one
+ * nx*ny*nz shot for `nsteps` steps, tiles tile_x*tile_y, z-chunks of
+ * `chunk` planes, `gap` places after each item's last dependency, steps
+ * overlapping if `overlap`.  *nitems receives the item count; items (if not
+ * NULL, room for *nitems on entry) receives per item (kind, step, chunk,
+ * tile, k0, k1).  ELA3D_ERR_INVALID_ARG on bad sizes or when an item would
+ * not follow the items it waits for.  No reference counterpart. */
+ela3d_status ela3d_flow_schedule_build(int32_t nx, int32_t ny, int32_t nz, int32_t tile_x, int32_t tile_y,
+                                       int32_t chunk, int32_t gap, int32_t overlap, int32_t nsteps,
+                                       int32_t *nitems, int32_t *items);
 ela3d_status ela3d_schedule_build(int32_t nx, int32_t ny, int32_t nz, int32_t tile_x, int32_t tile_y,
                                   int32_t schedule, int32_t chunk, int32_t max_blocks,
                                   int32_t *nitems, int32_t *nblocks,

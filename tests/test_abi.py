@@ -135,8 +135,11 @@ def _fp64_variant():
 BAD_TUNING = {
     "no_such_variant": lambda: {"variant": 10_000},
     "variant_of_other_precision": lambda: {"variant": _fp64_variant()},
-    "schedule_kind": lambda: {"schedule": 3},
+    "schedule_kind": lambda: {"schedule": 5},
     "negative_chunk": lambda: {"chunk": -2},
+    "dataflow_chunk_of_one_plane": lambda: {"schedule": 3, "chunk": 1},
+    "overlapping_dataflow_chunk_of_one_plane": lambda: {"schedule": 4, "chunk": 1},
+    "negative_lag": lambda: {"schedule": 3, "lag": -2},
 }
 
 

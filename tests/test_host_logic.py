@@ -82,3 +82,78 @@ def test_bytes_per_cell_definition():
     assert bytes_per_cell(256, 256, 256, 16)["step"] == pytest.approx(142.0)
     assert bytes_per_cell(256, 256, 256, 0)["step"] == 124.0
     assert bytes_per_cell(256, 256, 256, 16, word=8)["step"] == 284.0
+
+
+def _flow_deps(item, J, txs, tys):
+    """The items a dataflow item waits for, restated independently of the
+    library: stress (chunk j, tile t, step r) reads the velocities written by
+    velocity chunks j and j+1 of step r-1 on t and its four neighbours (and
+    overwrites the stresses they read); velocity (j, t, r) reads the
+    stresses of stress chunks j-1 and j of step r there."""
+    kind, step, chunk, tile = (int(v) for v in item[:4])
+    tx, ty = tile % txs, tile // txs
+    r = step - 1 if kind == 0 else step
+    if r < 0:
+        return []
+    chunks = [chunk, chunk + 1] if kind == 0 else [chunk, chunk - 1]
+    out = []
+    for x, y in ((tx, ty), (tx - 1, ty), (tx + 1, ty), (tx, ty - 1), (tx, ty + 1)):
+        if 0 <= x < txs and 0 <= y < tys:
+            for c in chunks:
+                if 0 <= c < J:
+                    out.append((1 - kind, r, c, y * txs + x))
+    return out
+
+
+@pytest.mark.parametrize("shape,tile,chunk,gap,overlap", [((101, 101, 101), (128, 7), 8, 152, False),
+                                                          ((101, 101, 101), (128, 7), 8, 152, True),
+                                                          ((70, 45, 33), (64, 14), 5, 3, True),
+                                                          ((40, 30, 9), (128, 3), 2, 1, False),
+                                                          ((40, 30, 9), (128, 3), 16, 40, True)])
+def test_flow_schedule_covers_every_update_once_in_dependency_order(built, shape, tile, chunk, gap, overlap):
+    from ela3d_gb300._abi import flow_schedule
+
+    nx, ny, nz = shape
+    K = 4
+    items = flow_schedule(nx, ny, nz, tile[0], tile[1], chunk, gap, overlap, K)
+    txs, tys = -(-nx // tile[0]), -(-ny // tile[1])
+    J = -(-nz // chunk)
+    keys = [tuple(int(v) for v in it[:4]) for it in items]
+    assert len(set(keys)) == len(keys) == K * 2 * J * txs * tys
+    pos = {k: q for q, k in enumerate(keys)}
+    # every cell plane is updated exactly once per half-step and step
+    for kind in (0, 1):
+        for r in range(K):
+            for t in range(txs * tys):
+                cover = np.zeros(nz, np.int32)
+                for it in items:
+                    if it[0] == kind and it[1] == r and it[3] == t:
+                        cover[it[4]:it[5]] += 1
+                assert np.all(cover == 1)
+    # velocity chunks sit one plane below the stress chunks
+    for it in items:
+        kind, _, j, _, k0, k1 = (int(v) for v in it)
+        if kind == 0:
+            assert (k0, k1) == (j * chunk, min((j + 1) * chunk, nz))
+        else:
+            assert k0 == max(j * chunk - 1, 0) and k1 == (nz if j == J - 1 else (j + 1) * chunk - 1)
+    for q, it in enumerate(items):
+        for d in _flow_deps(it, J, txs, tys):
+            assert pos[d] < q, (it, d)
+    # steps overlap only when asked to (and then they do, on deep grids)
+    first_of = {r: min(q for q, k in enumerate(keys) if k[1] == r) for r in range(K)}
+    last_of = {r: max(q for q, k in enumerate(keys) if k[1] == r) for r in range(K)}
+    overlapped = any(first_of[r + 1] < last_of[r] for r in range(K - 1))
+    if not overlap:
+        assert not overlapped
+    elif J >= 4:
+        assert overlapped
+
+
+@pytest.mark.parametrize("chunk,gap", [(1, 10), (4, 0), (0, 5)])
+def test_flow_schedule_rejects_bad_arguments(built, chunk, gap):
+    from ela3d_gb300 import Ela3dError
+    from ela3d_gb300._abi import flow_schedule
+
+    with pytest.raises(Ela3dError):
+        flow_schedule(40, 40, 40, 128, 7, chunk, gap, False, 2)
