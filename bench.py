@@ -216,20 +216,21 @@ def config_block(p, extra=None):
 
 
 # --------------------------------------------------------- CPU baseline --
-def cpu_reference_rate(p, cp, cs, rho, steps: int, procs: int) -> dict:
-    """Runs the reference CPU program (oracle/_ref) or, if it was not built,
-    the oracle's C restatement, as `procs` concurrent processes each doing
-    `steps` time steps of the shot; returns the aggregate rate."""
+def cpu_reference_rate(p, cp, cs, rho, steps: int, procs: int, fp64: bool = False) -> dict:
+    """Runs the reference CPU program (oracle/_ref; its float64 build with
+    fp64) or, if it was not built, the oracle's C restatement, as `procs`
+    concurrent processes each doing `steps` time steps of the shot; returns
+    the aggregate rate."""
     import oracle
 
-    exe = oracle.reference_binary(False)
+    exe = oracle.reference_binary(fp64)
     cells = p.cells
     warm = 1
     wd = tempfile.mkdtemp(prefix="ela3d_cpu_")
     try:
         if exe:
             for name, a in (("cp", cp), ("cs", cs), ("rho", rho)):
-                np.ascontiguousarray(a, np.float32).tofile(os.path.join(wd, f"m_{name}.bin"))
+                np.ascontiguousarray(a, np.float64 if fp64 else np.float32).tofile(os.path.join(wd, f"m_{name}.bin"))
             runs = []
             for q in range(procs):
                 d = os.path.join(wd, f"r{q}")
@@ -253,7 +254,7 @@ def cpu_reference_rate(p, cp, cs, rho, steps: int, procs: int) -> dict:
 
             ctx = mp.get_context("spawn")
             with ctx.Pool(procs) as pool:
-                res = pool.starmap(_port_worker, [(p, cp, cs, rho, steps)] * procs)
+                res = pool.starmap(_port_worker, [(p, cp, cs, rho, steps, fp64)] * procs)
             start = min(r[0] for r in res)
             end = max(r[1] for r in res)
             total = cells * steps * procs
@@ -265,8 +266,8 @@ def cpu_reference_rate(p, cp, cs, rho, steps: int, procs: int) -> dict:
     value = total / (end - start) / 1e9
     return {"value": value, "unit": METRIC, "cores": procs, "kind": kind,
             "sample": f"{procs} process(es) x {steps} time steps of the {p.nx}^3 shot "
-                      f"({'reference CPU program' if kind == 'reference' else 'C restatement'}), "
-                      f"{(end - start):.1f} s wall",
+                      f"({'reference CPU program' if kind == 'reference' else 'C restatement'}"
+                      f"{', float64 build' if fp64 else ''}), {(end - start):.1f} s wall",
             "seconds": end - start}
 
 
@@ -303,11 +304,11 @@ def reference_gpu_rate(n: int, steps: int, warm: int) -> dict:
     return {"value": None, "unavailable": f"reference GPU program exited {r.returncode} without a timing line"}
 
 
-def _port_worker(p, cp, cs, rho, steps):
+def _port_worker(p, cp, cs, rho, steps, fp64=False):
     import oracle
 
     t0 = time.perf_counter()
-    oracle.run(p.with_(rec=np.zeros((0, 3), np.int32)), cp, cs, rho, steps, want_fields=False)
+    oracle.run(p.with_(rec=np.zeros((0, 3), np.int32)), cp, cs, rho, steps, fp64=fp64, want_fields=False)
     t1 = time.perf_counter()
     return (t0, t1)
 
@@ -348,13 +349,18 @@ def run_ours(args, rank, world, local):
     plan.set_kernel_timing(True)
     plan.run_timed(args.kernel_steps)
     s_ms, v_ms, ns, nv = plan.kernel_timing()
+    f_ms, f_launches, f_steps = plan.flow_timing()
     plan.set_kernel_timing(False)
     plan.close()
     t_max = dist.max(ms / 1e3)
     value = cells * args.steps * world / t_max / 1e9
-    # kernels launched in the timed region: one step-counter set, 50-step
-    # graphs of 100 stencil launches plus a counter update, the rest direct
-    launches = 1 + (args.steps // 50) * 101 + (args.steps % 50) * 2
+    if f_launches:
+        # dataflow kernel: one launch per (up to) 50 steps
+        launches = -(-args.steps // 50)
+    else:
+        # kernels launched in the timed region: one step-counter set, 50-step
+        # graphs of 100 stencil launches plus a counter update, the rest direct
+        launches = 1 + (args.steps // 50) * 101 + (args.steps % 50) * 2
 
     # e2e: one whole shot through the C ABI from host arrays
     e2e = None
@@ -380,9 +386,16 @@ def run_ours(args, rank, world, local):
     peak, peak_kind = measured_peaks()
     kern = {}
     for name, tot, n, b in (("stress_kernel", s_ms, ns, bpc["stress"]), ("velocity_kernel", v_ms, nv, bpc["velocity"])):
-        per = tot / max(n, 1) / 1e3
+        if not n:
+            continue
+        per = tot / n / 1e3
         ach = b * cells / per / 1e9
         kern[name] = {"launches": n, "mean_ms": per * 1e3, "bytes_per_launch": b * cells, "achieved_gbs": ach}
+    if f_launches:
+        per_step = f_ms / f_steps / 1e3
+        kern["flow_kernel"] = {"launches": f_launches, "steps": f_steps, "mean_ms": f_ms / f_launches,
+                               "ms_per_step": per_step * 1e3, "bytes_per_step": bpc["step"] * cells,
+                               "achieved_gbs": bpc["step"] * cells / per_step / 1e9}
     dom = max(kern, key=lambda k: kern[k]["mean_ms"])
     traffic = profile_traffic(dom)
     roof = {"bound": "hbm", "kernel": dom, "achieved": kern[dom]["achieved_gbs"], "peak": peak, "unit": "GB/s",
@@ -393,10 +406,12 @@ def run_ours(args, rank, world, local):
     roof["step_frac"] = roof["step_achieved_gbs"] / peak
 
     extra = {}
+    if rank == 0 and world == 1 and not args.no_c0:
+        extra["c0"] = homogeneous_101(args)
     if args.large > 0 and rank == 0 and not args.no_batched:
         extra["large_grid"] = large_grid(args.large)
     if not args.no_batched:
-        extra["batched"] = batched_shots(args, value)   # shots split across ranks
+        extra["batched"] = batched_shots(args, value, e2e["value"] if e2e else None)   # shots split across ranks
         if world == 1:
             extra["uneven"] = uneven_batch(args)
             extra["serving"] = serving(args)
@@ -453,9 +468,87 @@ def large_grid(n: int, steps: int = 100) -> dict:
             "timing": "CUDA events around replayed 50-step graphs, built-in kernel choice"}
 
 
-def batched_shots(args, single_value: float) -> dict:
+def homogeneous_101(args) -> dict:
+    """The 101^3 homogeneous cube (10 PML cells, 1000 steps): FP32 and FP64
+    device rates with the built-in kernel choice, the HBM fraction at its
+    152.5 B (FP32) per cell-update, one full shot end to end, its accuracy
+    against the reference CPU program's own FP32 and FP64 runs of the same
+    shot (the committed fixture tests/golden/ref_homogeneous_101_full.npz),
+    and the reference program's FP32 and FP64 rates on one core."""
+    import ela3d_gb300 as E
+    from ela3d_gb300 import configs
+    from ela3d_gb300.metrics import bytes_per_cell
+
+    p, cp, cs, rho = configs.homogeneous_101()
+    cells = p.cells
+    peak, _ = measured_peaks()
+    steps = args.c0_steps
+    out = {"workload": "homogeneous_101: 101^3 cube, cp 3300 m/s, cs cp/1.732, rho 2800, dt 1.6e-3 s, "
+                       "1000-step shot, 10 PML cells, Ricker 7 Hz on vz at the centre, 11 receivers",
+           "metric": METRIC}
+    seis = {}
+    for tag, prec in (("fp32", 0), ("fp64", 1)):
+        q = p.with_(precision=prec)
+        bpc = bytes_per_cell(p.nx, p.ny, p.nz, p.npml, word=8 if prec else 4)["step"]
+        with E.Plan(q, cp, cs, rho) as pl:   # built-in kernel choice
+            pl.run(args.warmup)
+            ms = pl.run_timed(steps)
+            pl.set_kernel_timing(True)
+            pl.run(min(steps, 200))
+            f_ms, f_launches, f_steps = pl.flow_timing()
+            s_ms, v_ms, ns, nv = pl.kernel_timing()
+        rate = cells * steps / (ms / 1e3) / 1e9
+        row = {"value": rate, "ms_per_step": ms / steps, "steps_timed": steps, "bytes_per_cell_update": bpc,
+               "frac_of_hbm": rate * bpc / peak}
+        if f_launches:
+            per = f_ms / f_steps
+            row["kernel"] = {"name": "flow_kernel", "launches": f_launches, "steps": f_steps,
+                             "ms_per_step": per, "achieved_gbs": bpc * cells / per / 1e6,
+                             "frac": bpc * cells / per / 1e6 / peak}
+        elif ns:
+            per = (s_ms + v_ms) / ns
+            row["kernel"] = {"name": "stress_kernel + velocity_kernel", "launches": ns + nv,
+                             "ms_per_step": per, "achieved_gbs": bpc * cells / per / 1e6,
+                             "frac": bpc * cells / per / 1e6 / peak}
+        out[tag] = row
+        # one whole shot end to end through the C ABI from host arrays
+        t0 = time.perf_counter()
+        with E.Plan(q, cp, cs, rho) as pl:
+            pl.run(p.nstep)
+            seis[tag] = pl.seismograms(fp64=bool(prec))
+        row["e2e"] = {"value": cells * p.nstep / (time.perf_counter() - t0) / 1e9, "unit": METRIC,
+                      "what": f"full {p.nstep}-step shot: plan creation with model upload, run, seismogram read-back"}
+    # accuracy against the reference program's own runs of this shot
+    gold = os.path.join(ROOT, "tests", "golden", "ref_homogeneous_101_full.npz")
+    if os.path.exists(gold):
+        g = np.load(gold)
+        rel = lambda a, b: float(np.linalg.norm(np.asarray(a, np.float64) - b) / np.linalg.norm(b))  # noqa: E731
+        per = lambda a, b: max(rel(a[r], b[r]) for r in range(b.shape[0]) if np.any(b[r]))  # noqa: E731
+        r64 = g["seis_f64"]
+        out["accuracy_vs_reference_program"] = {
+            "what": "relative L2 of the seismograms against the reference CPU program's runs of the same shot",
+            "fp32_gpu_vs_fp64_program": {"all": rel(seis["fp32"], r64), "worst_seismogram": per(seis["fp32"], r64)},
+            "fp32_gpu_vs_fp32_program": {"all": rel(seis["fp32"], g["seis_f32"].astype(np.float64))},
+            "fp32_program_vs_fp64_program": {"all": rel(g["seis_f32"], r64), "worst_seismogram": per(g["seis_f32"], r64)},
+            "fp64_gpu_vs_fp64_program": {"all": rel(seis["fp64"], r64), "worst_seismogram": per(seis["fp64"], r64)}}
+    if not args.no_cpu_baseline:
+        for tag, fp64 in (("fp32", False), ("fp64", True)):
+            try:
+                out[f"cpu_reference_{tag}"] = cpu_reference_rate(p, cp, cs, rho, steps=args.c0_cpu_steps, procs=1,
+                                                                 fp64=fp64)
+            except Exception as e:  # reported, not fatal
+                out[f"cpu_reference_{tag}"] = {"value": None, "error": str(e)}
+    out["timing"] = ("CUDA events around the library's run (built-in kernel choice), after warm-up; kernel row: "
+                     "per-launch CUDA events of a second pass; e2e: wall clock")
+    return out
+
+
+def batched_shots(args, single_value: float, single_wall_value: float | None = None) -> dict:
     """64 shots of the 256^3 anticline (8 x 8 source grid at z = npml + 3,
-    one shared model) advanced together; graph replay, CUDA-event timing."""
+    one shared model) advanced together; graph replay, CUDA-event timing.
+    Compared with the single-shot path both device time to device time and
+    wall clock to wall clock (batch creation, run and read-back against one
+    whole shot's end-to-end rate)."""
     import ela3d_gb300 as E
     from ela3d_gb300 import configs
     from ela3d_gb300.metrics import bytes_per_cell
@@ -480,8 +573,10 @@ def batched_shots(args, single_value: float) -> dict:
         b.run(0)
         seis = [b.seismograms(q) for q in range(len(shots))]
         t_read = time.perf_counter() - t1
+        t_wall = time.perf_counter() - t0
     g = Group(world)
     value = g.sum(cells) * args.batch_steps / (g.max(ms) / 1e3) / 1e9
+    wall_value = g.sum(cells) * (args.warmup + args.batch_steps) / g.max(t_wall) / 1e9
     # two shots drawn by seed, checked against FP64
     pick = sorted(np.random.default_rng(2024).choice(len(shots), size=min(2, len(shots)), replace=False).tolist())
     steps_run = args.warmup + args.batch_steps
@@ -493,6 +588,9 @@ def batched_shots(args, single_value: float) -> dict:
             "metric": METRIC, "value": value, "steps_timed": args.batch_steps,
             "ms_per_step": ms / args.batch_steps, "single_shot_value": single_value,
             "ratio_vs_single_shot": value / single_value,
+            "wall_value": wall_value, "single_shot_wall_value": single_wall_value,
+            "ratios": {"device_over_device": value / single_value,
+                       "wall_over_wall": wall_value / single_wall_value if single_wall_value else None},
             "frac_of_hbm_at_142B": value * bpc / peak,
             "create_s": t_create, "readback_s": t_read,
             "tuning": tune_info, "fp64_check": check,
@@ -518,23 +616,33 @@ def uneven_batch(args) -> dict:
         tune_info = {"source": "ela3d_autotune on the whole batch", "candidates": cand, **tune}
     # each instance alone, with the better of the built-in and the tuned
     # kernel choice per instance
-    alone_default_s = alone_s = 0.0
+    alone_default_s = alone_s = alone_wall_s = 0.0
     for p, cp, cs, rho in inst:
         times = []
         for kw in [{}] + ([tune] if tune else []):
+            t0 = time.perf_counter()
             with E.Plan(p, cp, cs, rho, **kw) as pl:
                 pl.run(3)
                 times.append(pl.run_timed(steps) / 1e3)
+                pl.seismograms()
+            if not kw:   # wall clock of the plain path: creation, run, read-back
+                alone_wall_s += time.perf_counter() - t0
         alone_default_s += times[0]
         alone_s += min(times)
     alone = cells * steps / alone_s / 1e9
+    t0 = time.perf_counter()
     with E.Batch(inst, **tune) as b:
         b.run(3)
         ms = b.run_timed(steps)
         # two instances drawn by seed, as computed in the batch, against FP64
         pick = sorted(np.random.default_rng(2).choice(len(inst), 2, replace=False).tolist())
         seis = {q: b.seismograms(q) for q in pick}
+        for q in range(len(inst)):
+            b.seismograms(q)
+    batch_wall_s = time.perf_counter() - t0
     value = cells * steps / (ms / 1e3) / 1e9
+    wall_value = cells * (steps + 3) / batch_wall_s / 1e9
+    alone_wall = cells * (steps + 3) / alone_wall_s / 1e9
     sizes = [p.cells for p, *_ in inst]
     check = fp64_check([(f"instance {q}", *inst[q], 3 + steps, seis[q]) for q in pick])
     # algorithmic bytes of one step of every instance (each at its own PML share)
@@ -545,6 +653,8 @@ def uneven_batch(args) -> dict:
             "metric": METRIC, "value": value, "steps_timed": steps,
             "single_shot_sequential_value": alone, "single_shot_default_value": cells * steps / alone_default_s / 1e9,
             "ratio_vs_single_shot": value / alone, "tuning": tune_info,
+            "wall_value": wall_value, "single_shot_sequential_wall_value": alone_wall,
+            "ratios": {"device_over_device": value / alone, "wall_over_wall": wall_value / alone_wall},
             "bytes_per_cell_update": step_bytes / cells,
             "frac_of_hbm": step_bytes * steps / (ms / 1e3) / 1e9 / peak,
             "single_shot_frac_of_hbm": step_bytes * steps / alone_s / 1e9 / peak, "fp64_check": check,
@@ -654,6 +764,8 @@ def serving(args) -> dict:
             "single_shot_sequential_value": alone, "single_shot_default_value": total / alone_default_s / 1e9,
             "single_shot_sequential_wall_value": total / alone_wall / 1e9, "tuning": tune_info,
             "ratio_vs_single_shot": sat["gcells_per_s_wall"] / alone,
+            "ratios": {"device_over_device": sat["gcells_per_s_busy"] / alone,
+                       "wall_over_wall": sat["gcells_per_s_wall"] / (total / alone_wall / 1e9)},
             "bytes_per_cell_update": stream_bytes / total,
             "frac_of_hbm_busy": stream_bytes / busy_s / 1e9 / peak,
             "single_shot_frac_of_hbm": stream_bytes / alone_s / 1e9 / peak,
@@ -724,6 +836,10 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=50,
                     help="time steps of the one-core CPU baseline sample (about 15 s of CPU work)")
     ap.add_argument("--ref-steps-cap", type=int, default=20)
+    ap.add_argument("--no-c0", action="store_true", help="skip the 101^3 homogeneous-cube block")
+    ap.add_argument("--c0-steps", type=int, default=400, help="timed steps of the 101^3 cube")
+    ap.add_argument("--c0-cpu-steps", type=int, default=100,
+                    help="steps of the 101^3 one-core reference CPU samples (about 1-3 s each)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -324,6 +324,15 @@ TuneChoice default_choice(int fp64, int nx, int ny, int nz) {
     // y/z-slab memory variables into L2 ahead of use
     const double bytes = 12.0 * nx * ny * nz * (fp64 ? 8.0 : 4.0);
     if (bytes < 96.0 * (1 << 20)) c.prefetch = CTL_PF_X;
+    // FP32 grids whose arrays are within about twice the L2 run faster in
+    // the dataflow kernel with overlapping steps (measured: 101^3 +15% with
+    // 6-plane chunks, 128^3 +9% with 8-plane chunks; at 256^3 the two
+    // half-step kernels stay ahead)
+    if (!fp64 && v[i].flow && bytes < 256.0 * (1 << 20)) {
+      c.kind = kScheduleFlowOverlap;
+      c.chunk = bytes < 64.0 * (1 << 20) ? 6 : 8;
+      c.lag = 0;
+    }
   }
   return c;
 }

@@ -109,14 +109,20 @@ void tune_store(const std::vector<ela3d_params> &ps, const TuneChoice &c) {
 
 // Candidate schedules and prefetch modes for a workload: contiguous shares;
 // z-chunks of 6..128 planes round-robin; for batches also shot-interleaved
-// chunks; each with both memory-variable prefetches or the x slab's only.
-static std::vector<TuneChoice> schedules(int nshots) {
+// chunks; the dataflow kernel; each with both memory-variable prefetches or
+// the x slab's only.
+// The dataflow kernel (kinds 3 and 4) is tried with 4- to 16-plane chunks.
+static std::vector<TuneChoice> schedules(int nshots, bool flow) {
   std::vector<TuneChoice> v;
   for (int pf : {kPrefetchDefault, (int)CTL_PF_X}) {
     v.push_back({0, 0, 16, 0, pf});
     for (int ch : {6, 8, 10, 12, 16, 32, 64, 128}) v.push_back({0, 1, ch, 0, pf});
     if (nshots > 1)
       for (int ch : {8, 16}) v.push_back({0, 2, ch, 0, pf});
+    if (flow) {
+      for (int ch : {4, 6, 8, 16}) v.push_back({0, kScheduleFlowOverlap, ch, 0, pf, 0});
+      for (int ch : {8, 16}) v.push_back({0, kScheduleFlow, ch, 0, pf, 0});
+    }
   }
   return v;
 }
@@ -147,7 +153,7 @@ ela3d_status autotune(const std::vector<ela3d_params> &ps, const std::vector<con
     }
     if (st == ELA3D_ERR_OOM) return st;
     if (st != ELA3D_OK) continue;
-    for (TuneChoice c : schedules((int)ps.size())) {
+    for (TuneChoice c : schedules((int)ps.size(), vs[v].flow != nullptr)) {
       c.variant = v;
       st = eng->retune(c);
       if (st == ELA3D_OK) st = eng->enqueue(2);  // warm-up

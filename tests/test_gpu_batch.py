@@ -67,17 +67,17 @@ def test_batch_in_pieces_equals_one_run(built):
 
 
 def test_graph_replay_equals_direct_launches(built):
-    """Runs of 50+ steps replay a captured graph; with kernel timing on the
-    same steps launch directly."""
+    """Runs of 50+ steps of the two half-step kernels replay a captured
+    graph; with kernel timing on the same steps launch directly."""
     from ela3d_gb300 import Plan
 
     p, cp, cs, rho = shots()[0]
     p = p.with_(nstep=173)
-    with Plan(p, cp, cs, rho) as g:
+    with Plan(p, cp, cs, rho, schedule=1, chunk=8) as g:
         g.run(173)
         sg = g.seismograms()
         fg = g.field(2)
-    with Plan(p, cp, cs, rho) as d:
+    with Plan(p, cp, cs, rho, schedule=1, chunk=8) as d:
         d.set_kernel_timing(True)
         d.run(173)
         sd = d.seismograms()

@@ -131,16 +131,31 @@ def test_full_size_against_reference_program(built, name):
     for k, (per, whole) in res.items():
         print(f"{name} {k}: worst seismogram rel L2 {max(per):.2e}, all receivers {whole:.2e}")
     summ32, summ64 = make_golden.summarize(p, f32), make_golden.summarize(p, f64)
-    wave32 = max(rel_l2(summ32[k][c], g[f"{k}_f64"][c]) for k in ("slice_xy", "slice_yz") for c in range(9)
-                 if np.any(g[f"{k}_f64"][c]))
-    wave64 = max(rel_l2(summ64[k][c], g[f"{k}_f64"][c]) for k in ("slice_xy", "slice_yz") for c in range(9)
-                 if np.any(g[f"{k}_f64"][c]))
-    print(f"{name} final-field slices vs FP64 reference: FP32 GPU {wave32:.2e}, FP64 GPU {wave64:.2e}")
+    ref32 = {k: g[f"{k}_f32"] for k in ("slice_xy", "slice_yz")}
+
+    def slice_err(summ):   # worst component, and all nine together
+        per = max(rel_l2(summ[k][c], g[f"{k}_f64"][c]) for k in ("slice_xy", "slice_yz") for c in range(9)
+                  if np.any(g[f"{k}_f64"][c]))
+        both = rel_l2(np.concatenate([np.ravel(summ[k]) for k in ("slice_xy", "slice_yz")]),
+                      np.concatenate([np.ravel(g[f"{k}_f64"]) for k in ("slice_xy", "slice_yz")]))
+        return per, both
+
+    wave32, wave32_all = slice_err(summ32)
+    wave64, _ = slice_err(summ64)
+    wave_ref, wave_ref_all = slice_err(ref32)
+    print(f"{name} final-field slices vs FP64 reference program: FP32 GPU worst component {wave32:.2e} "
+          f"(all {wave32_all:.2e}), the program's own FP32 {wave_ref:.2e} (all {wave_ref_all:.2e}); "
+          f"FP64 GPU {wave64:.2e}")
     assert max(res["fp64_gpu_vs_fp64_ref"][0]) <= 1e-9
     assert wave64 <= 1e-9
     assert max(res["fp32_gpu_vs_fp64_ref"][0]) <= 1e-4
     assert res["fp32_gpu_vs_fp32_ref"][1] <= 1e-4
-    assert wave32 <= 1e-3
+    # the final wavefield in FP32: within 1e-3 over all components, and no
+    # component worse than three times the reference program's own FP32
+    # (after the wave has left through the C-PML, nearly silent components
+    # keep only round-off-sized residues)
+    assert wave32_all <= 1e-3
+    assert wave32 <= max(1e-3, 3 * wave_ref)
 
 
 def test_anticline_256_linear_in_the_source_amplitude(built):

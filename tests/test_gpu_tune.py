@@ -14,7 +14,8 @@ def test_autotune_picks_a_valid_choice_and_results_do_not_change(built, tmp_path
     p, cp, cs, rho = configs.anticline_256(nstep=60, n=96)
     best, ms, cand = E.autotune([(p, cp, cs, rho)], steps=5)
     n32 = sum(1 for v in E.variants() if not v.fp64 and v.loads == 0)   # TMA-loaded
-    assert cand == n32 * 18         # nine schedules x two prefetch modes for a single shot
+    # nine two-kernel and six dataflow schedules x two prefetch modes for a single shot
+    assert cand == n32 * 30
     assert 0 <= best.variant < len(E.variants()) and not E.variants()[best.variant].fp64
     assert ms > 0
     assert best.prefetch in (2, 6)
@@ -34,8 +35,9 @@ def test_autotune_batch_includes_interleaved_schedules(built):
     shots, cp, cs, rho = configs.anticline_256_shots(4, nstep=20, n=64)
     best, ms, cand = E.autotune([(s, cp, cs, rho) for s in shots], steps=3)
     n32 = sum(1 for v in E.variants() if not v.fp64 and v.loads == 0)   # TMA-loaded
-    assert cand == n32 * 22         # eleven schedules x two prefetch modes for a batch
-    assert best.schedule in (0, 1, 2)
+    # eleven two-kernel and six dataflow schedules x two prefetch modes for a batch
+    assert cand == n32 * 34
+    assert best.schedule in (0, 1, 2, 3, 4)
 
 
 CHILD = r"""
