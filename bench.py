@@ -271,15 +271,23 @@ def cpu_reference_rate(p, cp, cs, rho, steps: int, procs: int, fp64: bool = Fals
             "seconds": end - start}
 
 
-def reference_gpu_rate(n: int, steps: int, warm: int) -> dict:
-    """The reference's own FP32 GPU program (seismicCPML_3d_isotropic_cudazerocopy.cu,
-    built by oracle/make_ref.py into oracle/_ref) on this GPU: an n^3 grid,
-    `warm` untimed steps, then `steps` timed by the program (file output off).
-    Its own constant medium and first-derivative-of-Gaussian source; the
-    kernels are the reference's, unchanged."""
-    exe = os.path.join(ROOT, "oracle", "_ref", "ref_gpu_f32")
+REF_GPU_PROGRAMS = {
+    "ref_gpu_f32": "the reference's FP32 CUDA program (seismicCPML_3d_isotropic_cudazerocopy.cu: five stencil "
+                   "kernels per step plus gather and source, 8x8x8-thread blocks, arrays in device memory)",
+    "ref_gpu_f64": "the reference's FP64 CUDA program (elatic_3d_unified_cuda_memory.cu: five stencil kernels "
+                   "per step plus gather and source, 5x5x5-thread blocks, arrays in managed memory prefetched "
+                   "to the GPU before the loop)",
+}
+
+
+def reference_gpu_rate(n: int, steps: int, warm: int, program: str = "ref_gpu_f32") -> dict:
+    """One of the reference's own GPU programs (built by oracle/make_ref.py
+    into oracle/_ref) on this GPU: an n^3 grid, `warm` untimed steps, then
+    `steps` timed by the program (file output off).  Its own constant medium
+    and source; the kernels are the reference's, unchanged."""
+    exe = os.path.join(ROOT, "oracle", "_ref", program)
     if not os.path.exists(exe):
-        return {"value": None, "unavailable": "reference GPU program not built (oracle/_ref/ref_gpu_f32)"}
+        return {"value": None, "unavailable": f"reference GPU program not built (oracle/_ref/{program})"}
     wd = tempfile.mkdtemp(prefix="ela3d_refgpu_")
     try:
         r = subprocess.run([exe, str(n), str(steps + warm), str(warm), "0"], cwd=wd, capture_output=True,
@@ -297,10 +305,8 @@ def reference_gpu_rate(n: int, steps: int, warm: int) -> dict:
             secs = float(got["seconds"])
             return {"value": n ** 3 * int(got["steps"]) / secs / 1e9, "unit": METRIC,
                     "ms_per_step": secs * 1e3 / int(got["steps"]),
-                    "what": f"the reference's FP32 CUDA program (seismicCPML_3d_isotropic_cudazerocopy.cu: five "
-                            f"stencil kernels per step plus gather and source, 8x8x8-thread blocks), {n}^3, "
-                            f"{warm} warm-up + {got['steps']} timed steps, wall clock around its loop, file "
-                            f"output off"}
+                    "what": f"{REF_GPU_PROGRAMS[program]}, {n}^3, {warm} warm-up + {got['steps']} timed steps, "
+                            f"wall clock around its loop, file output off"}
     return {"value": None, "unavailable": f"reference GPU program exited {r.returncode} without a timing line"}
 
 
@@ -417,7 +423,7 @@ def run_ours(args, rank, world, local):
             extra["serving"] = serving(args)
 
     cpu = None
-    ref_gpu = None
+    ref_gpu = ref_gpu64 = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         try:
             cpu = cpu_reference_rate(p, cp, cs, rho, steps=args.cpu_steps, procs=1)
@@ -429,6 +435,15 @@ def run_ours(args, rank, world, local):
                 ref_gpu["ours_over_reference_gpu"] = value / ref_gpu["value"]
         except Exception as e:  # reported, not fatal
             ref_gpu = {"value": None, "error": str(e)}
+        try:
+            # an edge divisible by its 5-thread blocks, so they cover the grid
+            ref_gpu64 = reference_gpu_rate(255, steps=50, warm=5, program="ref_gpu_f64")
+            ours64 = fp64_rate(255, steps=50)
+            ref_gpu64["ours_fp64_same_grid"] = ours64
+            if ref_gpu64.get("value"):
+                ref_gpu64["ours_fp64_over_reference_gpu_fp64"] = ours64["value"] / ref_gpu64["value"]
+        except Exception as e:  # reported, not fatal
+            ref_gpu64 = {"value": None, "error": str(e)}
     dist.close()
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
@@ -437,7 +452,8 @@ def run_ours(args, rank, world, local):
                 "data": "synthetic (seeded anticline model)",
                 "config": config_block(p, {"steps_timed": args.steps, "tuning": tune_info}),
                 "e2e": e2e, "gpu_launches": int(launches * world), "roofline": roof,
-                "cpu_baseline": cpu, "reference_gpu_program": ref_gpu, "clocks": clk, "accuracy": accuracy}
+                "cpu_baseline": cpu, "reference_gpu_program": ref_gpu, "reference_gpu_program_fp64": ref_gpu64,
+                "clocks": clk, "accuracy": accuracy}
         line.update(extra)
         print(json.dumps(line), flush=True)
 
@@ -466,6 +482,23 @@ def large_grid(n: int, steps: int = 100) -> dict:
             "value": value, "steps_timed": steps, "ms_per_step": ms / steps, "bytes_per_cell_update": bpc,
             "frac_of_hbm": value * 1e9 * bpc / 1e9 / peak, "device_bytes": int(info.device_bytes),
             "timing": "CUDA events around replayed 50-step graphs, built-in kernel choice"}
+
+
+def fp64_rate(n: int, steps: int) -> dict:
+    """This library's FP64 build on an n^3 anticline (model generated on the
+    GPU), built-in kernel choice: the rate beside the reference's FP64 GPU
+    program at the same grid size."""
+    import ela3d_gb300 as E
+    from ela3d_gb300 import media
+
+    npml, f0 = 16, 12.0
+    p = E.ShotParams(nx=n, ny=n, nz=n, nstep=steps + 5, dt=1e-3, npml=npml, f0=f0, t0=1.2 / f0, src=(n // 2, n // 2, npml + 3),
+                     precision=1)
+    with E.Plan.from_model(p, media.anticline_256_spec(n)) as plan:
+        plan.run(5)
+        ms = plan.run_timed(steps)
+    return {"value": n ** 3 * steps / (ms / 1e3) / 1e9, "unit": METRIC, "ms_per_step": ms / steps,
+            "what": f"this library's FP64 build, {n}^3 anticline, {steps} steps, CUDA events"}
 
 
 def homogeneous_101(args) -> dict:

@@ -1,8 +1,10 @@
-"""Build recipe for the CUDA library.
+"""Build recipe for the CUDA library and its command-line runner.
 
-``build_library()`` compiles every translation unit under ``csrc/`` for
+``build_library()`` compiles every CUDA translation unit under ``csrc/`` for
 sm_103a in parallel and links ``_build/libela3d.so`` (in-tree, git-ignored).
-Rebuilds only when a source is newer than the output.
+``build_runner()`` compiles the C++ runner ``csrc/ela3d_run.cpp`` (host code
+on the C ABI) into ``_build/ela3d_run``, linked to that library.  Both
+rebuild only when a source is newer than the output.
 """
 from __future__ import annotations
 
@@ -63,5 +65,19 @@ def build_library(verbose: bool = False) -> str:
     return LIB
 
 
+RUNNER = os.path.join(OUT, "ela3d_run")
+
+
+def build_runner() -> str:
+    """The C++ runner; the library is found next to it at run time."""
+    src = os.path.join(CSRC, "ela3d_run.cpp")
+    header = os.path.join(ROOT, "include", "ela3d.h")
+    if _newer([src, header, LIB], RUNNER):
+        subprocess.run(["g++", "-O2", "-std=c++17", src, "-I", os.path.join(ROOT, "include"), "-L", OUT, "-lela3d",
+                        "-Wl,-rpath,$ORIGIN", "-o", RUNNER], check=True)
+    return RUNNER
+
+
 if __name__ == "__main__":
     print(build_library(verbose=True))
+    print(build_runner())

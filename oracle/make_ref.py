@@ -40,6 +40,18 @@ after the warm-up steps and the launch status are printed after the loop.
 Its kernels' indices were checked by reading for cubic grids whose edge is a
 multiple of 8: every neighbour access stays inside the arrays.
 
+And the reference's FP64 GPU program ``elatic_3d_unified_cuda_memory.cu``
+(all arrays in managed memory, seven kernels per step with 5x5x5-thread
+blocks), with a patch that changes no kernel and no launch shape: grid edge,
+steps and warm-up from the command line (:499-501,:530), the per-step
+receiver text, the snapshots and the initial model dump switched off by the
+same flag (:583-591,:1110,:1154), its thirty managed grid arrays prefetched
+to the GPU before the loop (first touched by the host, they would otherwise
+migrate page by page inside the timed steps), and the same timing line.  Its
+kernels' indices were checked by reading: every neighbour access is guarded
+by the update ranges; for an edge divisible by 5 the blocks cover the grid
+exactly.
+
 Usage: python oracle/make_ref.py [--ref DIR] [--no-build]
 (DIR defaults to ELA3D_REFERENCE_DIR, else a ``reference`` directory beside
 this repository.)
@@ -188,6 +200,59 @@ def patch_gpu(src: str) -> str:
     return s
 
 
+GPU64_REF_NAME = "elatic_3d_unified_cuda_memory.cu"
+# the managed grid arrays of the FP64 GPU program (prefetched to the device
+# before its time loop, so that the loop times its kernels and not page
+# migration)
+_GPU64_ARRAYS = ("cp", "cs", "rho", "vx", "vy", "vz", "sigmaxx", "sigmaxy", "sigmayy", "sigmazz", "sigmaxz",
+                 "sigmayz", "memory_dvx_dx", "memory_dvx_dy", "memory_dvx_dz", "memory_dvy_dx", "memory_dvy_dy",
+                 "memory_dvy_dz", "memory_dvz_dx", "memory_dvz_dy", "memory_dvz_dz", "memory_dsigmaxx_dx",
+                 "memory_dsigmayy_dy", "memory_dsigmazz_dz", "memory_dsigmaxy_dx", "memory_dsigmaxy_dy",
+                 "memory_dsigmaxz_dx", "memory_dsigmaxz_dz", "memory_dsigmayz_dy", "memory_dsigmayz_dz")
+
+
+def patch_gpu64(src: str) -> str:
+    """The FP64 GPU program (managed memory, 5x5x5-thread blocks), made
+    runnable at a given size without file I/O in the timed loop; kernels and
+    launch shapes untouched.  Its managed grid arrays, first touched by the
+    host, are prefetched to the GPU before the loop."""
+    s = src.replace("\r\n", "\n")
+    s = _sub(s, "#include <iomanip>", "#include <iomanip>\n#include <chrono>")
+    s = _sub(s, "int main(void) {", "int main(int argc, char **argv) {\n"
+             "\tconst int ref_n = argc > 1 ? atoi(argv[1]) : 373;\n"
+             "\tconst int ref_warm = argc > 3 ? atoi(argv[3]) : 0;\n"
+             "\tconst int ref_io = argc > 4 ? atoi(argv[4]) : 1;")
+    s = _sub(s, "\tNIMX = 373;\n\tNIMY = 373;\n\tNIMZ = 373;", "\tNIMX = ref_n;\n\tNIMY = ref_n;\n\tNIMZ = ref_n;")
+    s = _sub(s, "int NSTEP = 200;", "int NSTEP = argc > 2 ? atoi(argv[2]) : 200;")
+    s = _sub(s, "foutt.write((char *)&rho[ijk], sizeof rho[ijk]);",
+             "if (ref_io) foutt.write((char *)&rho[ijk], sizeof rho[ijk]);")
+    arrays = ", ".join(_GPU64_ARRAYS)
+    s = _sub(s, "\tdim3 threads;\n",
+             "\t{\n\t\tint ref_dev = 0;\n\t\tHANDLE_ERROR(cudaGetDevice(&ref_dev));\n"
+             "\t\tcudaMemLocation ref_loc;\n\t\tref_loc.type = cudaMemLocationTypeDevice;\n"
+             "\t\tref_loc.id = ref_dev;\n"
+             f"\t\tdouble *ref_arrays[] = {{{arrays}}};\n"
+             "\t\tfor (double *ref_a : ref_arrays)\n"
+             "\t\t\tHANDLE_ERROR(cudaMemPrefetchAsync(ref_a, sizeof(double)*NIMX*NIMY*NIMZ, ref_loc, 0, 0));\n"
+             "\t\tHANDLE_ERROR(cudaDeviceSynchronize());\n\t}\n"
+             "\tdim3 threads;\n")
+    s = _sub(s, "\tfor (int it = 1; it <= NSTEP; it++){",
+             "\tstd::chrono::steady_clock::time_point ref_t0 = std::chrono::steady_clock::now();\n"
+             "\tfor (int it = 1; it <= NSTEP; it++){\n"
+             "\t\tif (it == ref_warm + 1) { cudaDeviceSynchronize(); ref_t0 = std::chrono::steady_clock::now(); }")
+    s = _sub(s, "if (fmod(it, sampgat) == 0) {", "if (ref_io && fmod(it, sampgat) == 0) {")
+    s = _sub(s, "if (fmod(it, IT_OUTPUT) == 0){", "if (ref_io && fmod(it, IT_OUTPUT) == 0){")
+    s = _sub(s, "\tchar nmfilesx[20], nmfilesy[20], nmfilesz[20];",
+             "\t{\n\t\tcudaError_t ref_e = cudaDeviceSynchronize();\n"
+             "\t\tif (ref_e == cudaSuccess) ref_e = cudaGetLastError();\n"
+             "\t\tconst double ref_s = std::chrono::duration<double>(std::chrono::steady_clock::now() - ref_t0).count();\n"
+             "\t\tprintf(\"ELA3D_REF_GPU n %d steps %d seconds %.9f status %d\\n\", NIMX, NSTEP - ref_warm, ref_s,"
+             " (int)ref_e);\n\t}\n"
+             "\tif (!ref_io) return 0;\n"
+             "\tchar nmfilesx[20], nmfilesy[20], nmfilesz[20];")
+    return s
+
+
 def gpu_compiler_cmd(src: str, exe: str) -> list[str]:
     # 512-thread blocks: at most 128 registers a thread (the kernels' launches
     # are not error-checked by the program, so the cap keeps every launch valid)
@@ -230,6 +295,11 @@ def generate(ref_dir: str) -> None:
         with open(gpu, "r", encoding="latin-1") as f:
             g = patch_gpu(f.read())
         _write_if_changed(os.path.join(OUT, "ref_gpu_f32.cu"), g)
+    gpu64 = os.path.join(ref_dir, GPU64_REF_NAME)
+    if os.path.exists(gpu64):
+        with open(gpu64, "r", encoding="latin-1") as f:
+            g = patch_gpu64(f.read())
+        _write_if_changed(os.path.join(OUT, "ref_gpu_f64.cu"), g)
 
 
 def build() -> list[str]:
@@ -242,10 +312,11 @@ def build() -> list[str]:
             continue
         exe = os.path.join(OUT, f"ref_{v}")
         procs.append((exe, subprocess.Popen(compiler_cmd(src, exe))))
-    gsrc = os.path.join(OUT, "ref_gpu_f32.cu")
-    if os.path.exists(gsrc) and shutil.which("nvcc"):
-        exe = os.path.join(OUT, "ref_gpu_f32")
-        procs.append((exe, subprocess.Popen(gpu_compiler_cmd(gsrc, exe))))
+    for name in ("ref_gpu_f32", "ref_gpu_f64"):
+        gsrc = os.path.join(OUT, name + ".cu")
+        if os.path.exists(gsrc) and shutil.which("nvcc"):
+            exe = os.path.join(OUT, name)
+            procs.append((exe, subprocess.Popen(gpu_compiler_cmd(gsrc, exe))))
     for exe, p in procs:
         if p.wait() != 0:
             raise RuntimeError(f"building {exe} failed")
