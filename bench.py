@@ -810,6 +810,184 @@ def serving(args) -> dict:
                       "built-in choice only; wall value: built-in choice, plan creation and read-back included)"}
 
 
+# ------------------------------------------------- full-size configs --
+def single_shot_rates(tune: dict) -> dict:
+    """One whole 2000-step 256^3 anticline shot: device rate (CUDA events)
+    and end-to-end wall rate (plan creation with the model upload, run,
+    seismogram read-back)."""
+    import ela3d_gb300 as E
+
+    p, cp, cs, rho = workload()
+    t0 = time.perf_counter()
+    with E.Plan(p, cp, cs, rho, **tune) as pl:
+        ms = pl.run_timed(p.nstep)
+        pl.seismograms()
+    wall = time.perf_counter() - t0
+    return {"value": p.cells * p.nstep / (ms / 1e3) / 1e9, "wall_value": p.cells * p.nstep / wall / 1e9,
+            "steps": p.nstep}
+
+
+def uneven_full(args) -> dict:
+    """The 48 uneven grids each run to t = 2 s (its own nstep), all in one
+    batch (shots retire at their nstep) against each alone for its nstep."""
+    import ela3d_gb300 as E
+    from ela3d_gb300 import configs
+    from ela3d_gb300.metrics import bytes_per_cell
+
+    inst = configs.uneven_batch(count=args.uneven_count)
+    work = float(sum(p.cells * p.nstep for p, *_ in inst))
+    tune, tune_info = {}, {"source": "built-in default"}
+    if not args.no_autotune:
+        best, _, cand = E.autotune(inst, steps=3)
+        tune = best.as_dict()
+        tune_info = {"source": "ela3d_autotune on the whole batch", "candidates": cand, **tune}
+    alone_s = alone_wall_s = 0.0
+    for p, cp, cs, rho in inst:
+        t0 = time.perf_counter()
+        with E.Plan(p, cp, cs, rho) as pl:   # the plain path: built-in choice
+            alone_s += pl.run_timed(p.nstep) / 1e3
+            pl.seismograms()
+        alone_wall_s += time.perf_counter() - t0
+    longest = max(p.nstep for p, *_ in inst)
+    pick = sorted(np.random.default_rng(2).choice(len(inst), 2, replace=False).tolist())
+    t0 = time.perf_counter()
+    with E.Batch(inst, **tune) as b:
+        ms = b.run_timed(longest)
+        seis = {q: b.seismograms(q) for q in range(len(inst))}
+    wall_s = time.perf_counter() - t0
+    check = fp64_check([(f"instance {q}", *inst[q], inst[q][0].nstep, seis[q]) for q in pick])
+    step_bytes = sum(p.cells * p.nstep * bytes_per_cell(p.nx, p.ny, p.nz, p.npml)["step"] for p, *_ in inst)
+    peak, _ = measured_peaks()
+    value = work / (ms / 1e3) / 1e9
+    alone = work / alone_s / 1e9
+    return {"workload": f"uneven_batch at its named size: {len(inst)} grids, each to t = 2 s "
+                        f"({min(p.nstep for p, *_ in inst)}-{longest} steps), FP32",
+            "metric": METRIC, "value": value, "wall_value": work / wall_s / 1e9, "cell_updates": work,
+            "single_shot_sequential_value": alone, "single_shot_sequential_wall_value": work / alone_wall_s / 1e9,
+            "ratios": {"device_over_device": value / alone, "wall_over_wall": alone_wall_s / wall_s},
+            "frac_of_hbm": step_bytes / (ms / 1e3) / 1e9 / peak, "tuning": tune_info, "fp64_check": check,
+            "timing": "device: CUDA events around the batch run (shots retire at their nstep) and around each "
+                      "instance alone (built-in choice); wall: creation, run and read-back of all instances"}
+
+
+def serving_full(args) -> dict:
+    """The serving stream at its named size: 2000 requests of 2 s simulated
+    time (lognormal edges in [64, 384], per-request seeded models generated
+    on the GPU at admission), all submitted at once (saturation) and with
+    Poisson arrivals at a fraction of that rate; every 50th request re-run
+    alone in FP64; the plain single-shot path timed on every 10th request."""
+    import threading
+
+    import ela3d_gb300 as E
+    from ela3d_gb300 import configs
+    from ela3d_gb300.metrics import bytes_per_cell
+
+    n = args.full_serve_count
+    reqs = [configs.serving_request_spec(1000 + q, t_end=2.0) for q in range(n)]
+    work = [float(p.cells * p.nstep) for p, _ in reqs]
+    total = sum(work)
+    tune, tune_info = {}, {"source": "built-in default"}
+    if not args.no_autotune:
+        # tuned on eight requests spread over the stream, with host models
+        sample = [configs.serving_request(1000 + q, t_end=0.25) for q in range(0, n, max(1, n // 8))][:8]
+        best, _, cand = E.autotune(sample, steps=5)
+        tune = best.as_dict()
+        tune_info = {"source": "ela3d_autotune on eight requests", "candidates": cand, **tune}
+    # the plain single-shot path on every 10th request
+    sub = list(range(0, n, 10))
+    sub_work = sum(work[q] for q in sub)
+    alone_s = alone_wall_s = 0.0
+    for q in sub:
+        p, spec = reqs[q]
+        t0 = time.perf_counter()
+        with E.Plan.from_model(p, spec) as pl:
+            alone_s += pl.run_timed(p.nstep) / 1e3
+            pl.seismograms()
+        alone_wall_s += time.perf_counter() - t0
+    alone, alone_wall = sub_work / alone_s / 1e9, sub_work / alone_wall_s / 1e9
+    rows, served, capacity = [], {}, None
+    rng = np.random.default_rng(7)
+    for load in args.full_serve_loads:
+        with E.Server(steps_per_round=args.serve_round, **tune) as srv:
+            gaps = rng.exponential(1.0 / (load * capacity), n) if load > 0 and capacity else None
+            tickets = []
+
+            def client():
+                for q, (p, spec) in enumerate(reqs):
+                    if gaps is not None:
+                        time.sleep(gaps[q])
+                    tickets.append(srv.submit_model(p, spec))
+
+            t_start = time.perf_counter()
+            th = threading.Thread(target=client)
+            th.start()
+            th.join()
+            for q, t in enumerate(tickets):
+                srv.wait(t)
+                if load == 0 and q % 50 == 0:
+                    served[q] = srv.read(t)
+                srv.release(t)
+            wall = time.perf_counter() - t_start
+            st = srv.stats()
+        if load == 0:
+            capacity = n / wall
+        rows.append({"offered_load": "saturation" if load == 0 else load,
+                     "arrival_rate_per_s": None if load == 0 else load * capacity, "requests": n,
+                     "gcells_per_s_wall": total / wall / 1e9, "gcells_per_s_busy": total / st["busy_seconds"] / 1e9,
+                     "p50_latency_s": st["latency_p50_s"], "p99_latency_s": st["latency_p99_s"],
+                     "max_latency_s": st["latency_max_s"], "rounds": st["rounds"], "failed": st["failed"],
+                     "wall_s": wall})
+    sat = rows[0]
+    # every 50th request alone in FP64 (model generated on the device)
+    chk = []
+    for q, s32 in served.items():
+        p, spec = reqs[q]
+        with E.Plan.from_model(p.with_(precision=1), spec) as pl:
+            pl.run(p.nstep)
+            s64 = pl.seismograms(fp64=True)
+        a, b = s32.astype(np.float64), s64
+        chk.append(float(np.linalg.norm(a - b) / np.linalg.norm(b)))
+    stream_bytes = sum(p.cells * p.nstep * bytes_per_cell(p.nx, p.ny, p.nz, p.npml)["step"] for p, _ in reqs)
+    peak, _ = measured_peaks()
+    sizes = [p.cells for p, _ in reqs]
+    return {"workload": f"serving stream at its named size: {n} requests of 2 s simulated time (seeded lognormal "
+                        f"edges in [64, 384], {min(sizes) / 1e6:.2f}-{max(sizes) / 1e6:.1f} Mcells, models "
+                        f"generated on the GPU at admission), FP32",
+            "metric": METRIC, "value": sat["gcells_per_s_wall"], "cell_updates": total,
+            "p50_latency_s": sat["p50_latency_s"], "p99_latency_s": sat["p99_latency_s"],
+            "single_shot_sequential_value": alone, "single_shot_sequential_wall_value": alone_wall,
+            "single_shot_sample": f"every 10th request ({len(sub)}) alone, built-in choice",
+            "ratios": {"device_over_device": sat["gcells_per_s_busy"] / alone,
+                       "wall_over_wall": sat["gcells_per_s_wall"] / alone_wall},
+            "frac_of_hbm_busy": stream_bytes / (total / (sat["gcells_per_s_busy"] * 1e9)) / 1e9 / peak,
+            "sweep": rows, "tuning": tune_info, "steps_per_round": args.serve_round,
+            "fp64_check": {"what": "every 50th request's FP32 seismograms as served vs the request re-run alone in "
+                                   "FP64 (relative L2)", "requests": len(chk), "max_rel_l2": max(chk) if chk else None,
+                           "median_rel_l2": float(np.median(chk)) if chk else None}}
+
+
+def run_full(args) -> None:
+    """--full: the named configurations at their full sizes (opt-in; minutes
+    of GPU time each), one JSON line."""
+    import ela3d_gb300 as E
+
+    E.select_device(0)
+    clocks = ClockSampler(0)
+    clocks.start()
+    out = {"metric": METRIC, "full_configs": {}}
+    if "batched" in args.full:
+        single = single_shot_rates({})
+        args.batch_steps = 2000
+        out["full_configs"]["batched"] = batched_shots(args, single["value"], single["wall_value"])
+        out["full_configs"]["batched"]["single_shot"] = single
+    if "uneven" in args.full:
+        out["full_configs"]["uneven"] = uneven_full(args)
+    if "serve" in args.full:
+        out["full_configs"]["serving"] = serving_full(args)
+    out["clocks"] = clocks.stop()
+    print(json.dumps(out), flush=True)
+
+
 def run_reference(args, rank, world, local):
     if rank != 0:
         return
@@ -873,10 +1051,20 @@ def main():
     ap.add_argument("--c0-steps", type=int, default=400, help="timed steps of the 101^3 cube")
     ap.add_argument("--c0-cpu-steps", type=int, default=100,
                     help="steps of the 101^3 one-core reference CPU samples (about 1-3 s each)")
+    ap.add_argument("--full", nargs="+", default=[], choices=["batched", "uneven", "serve"],
+                    help="instead of the default line: the named batched, uneven and serving configurations at "
+                         "their full sizes (64 shots x 2000 steps; 48 grids to t = 2 s; 2000 requests of 2 s)")
+    ap.add_argument("--full-serve-count", type=int, default=2000)
+    ap.add_argument("--full-serve-loads", type=float, nargs="+", default=[0.0, 0.8],
+                    help="offered loads of the full serving stream (0 = all submitted at once)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     rank, world, local = dist_env()
+    if args.full:
+        if rank == 0:
+            run_full(args)
+        return
     if args.impl == "reference":
         run_reference(args, rank, world, local)
     else:

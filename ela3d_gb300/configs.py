@@ -15,6 +15,8 @@
 - serving_request: one request of a stream with lognormal edges clipped to
   [64, 384] (mu = ln 128, sigma = 0.45), per-request seed for model, source
   and receiver line; npml U{10..20}, at most (min edge - 10) / 2.
+  serving_request_spec: the same request with its model generated on the
+  device.
 Edge lengths, positions and seeds are those the configs name; anything they
 leave open is fixed here and stated in the docstring.
 """
@@ -96,6 +98,39 @@ def uneven_batch(count: int = 48, seed: int = 1, t_end: float = 2.0, precision: 
                        src=(sx, sy, sz), rec=_line(sx, nx, 201, sy, sz), precision=precision)
         out.append((p, cp, cs, rho))
     return out
+
+
+def serving_request_spec(seed: int, t_end: float = 2.0, precision: int = FP32, lo: int = 64, hi: int = 384,
+                         mu: float = math.log(128.0), sigma: float = 0.45, f0: float = 10.0):
+    """The same request as serving_request(seed) -- the same draws from the
+    same seed, so the same grid, layers, time step, source and receivers --
+    with its model as a device-generator spec (ela3d_model_spec) instead of
+    host arrays: the layered dome of media.random_anticline, generated on
+    the GPU at admission.  Returns (ShotParams, spec)."""
+    rng = np.random.default_rng(seed)
+    edges = [int(min(max(round(rng.lognormal(mu, sigma)), lo), hi)) for _ in range(3)]
+    nx, ny, nz = edges
+    npml = min(int(rng.integers(10, 21)), (min(edges) - 10) // 2)
+    # media.random_anticline's draws, in its order
+    nl = int(rng.integers(3, 7))
+    cps = np.sort(rng.uniform(1800.0, 4500.0, nl))
+    ratios = rng.uniform(1.6, 2.0, nl)
+    depths = np.sort(rng.uniform(0.15, 0.9, nl - 1)) * nz
+    amp = float(rng.uniform(0.05, 0.2)) * nz
+    sig = float(rng.uniform(0.15, 0.35)) * min(nx, ny)
+    # nl - 1 interfaces; the device counts interfaces crossed, so a last one
+    # far below the grid keeps the deepest layer to the bottom
+    spec = media.dome_spec(nx, ny, list(depths) + [1e9], [float(c) for c in cps], [float(r) for r in ratios], amp,
+                           sig)
+    # (the host model's fastest velocity is the float32 of the layer's)
+    dt = cfl_dt(float(np.float32(cps.max())), 10.0, 10.0, 10.0, 0.5)
+    nstep = int(math.ceil(t_end / dt))
+    sx = int(rng.integers(npml + 2, nx - npml - 2))
+    sy = int(rng.integers(npml + 2, ny - npml - 2))
+    sz = npml + 3
+    p = ShotParams(nx=nx, ny=ny, nz=nz, nstep=nstep, dt=dt, npml=npml, f0=f0, t0=1.2 / f0, src=(sx, sy, sz),
+                   rec=_line(sx, nx, min(201, nx), sy, sz), precision=precision)
+    return p, spec
 
 
 def serving_request(seed: int, t_end: float = 2.0, precision: int = FP32, lo: int = 64, hi: int = 384,

@@ -153,7 +153,9 @@ ela3d_status autotune(const std::vector<ela3d_params> &ps, const std::vector<con
     }
     if (st == ELA3D_ERR_OOM) return st;
     if (st != ELA3D_OK) continue;
-    for (TuneChoice c : schedules((int)ps.size(), vs[v].flow != nullptr)) {
+    // the dataflow list is rebuilt on the host whenever shots join or
+    // retire, which batches and servers do: it is tried for single shots
+    for (TuneChoice c : schedules((int)ps.size(), vs[v].flow != nullptr && ps.size() == 1)) {
       c.variant = v;
       st = eng->retune(c);
       if (st == ELA3D_OK) st = eng->enqueue(2);  // warm-up

@@ -272,7 +272,10 @@ typedef struct ela3d_tuning {
  * after them, while their results are still in L2; schedule 3 keeps the
  * time steps in sequence, schedule 4 lets a step start where the previous
  * one is done.  Results are bit-identical to schedules 0-2.  Shots with an
- * explosive source run the two-kernel path with schedule 1. */
+ * explosive source run the two-kernel path with schedule 1.  The work list
+ * is built on the host for the shots running, again whenever shots join or
+ * retire, so these schedules suit a plan or a batch of shots that run
+ * together; the autotuner tries them for single shots. */
 
 /* Times every compiled variant with the candidate schedules on these shots
  * (`steps` time steps each, after a warm-up) and returns the fastest choice;

@@ -35,9 +35,10 @@ def test_autotune_batch_includes_interleaved_schedules(built):
     shots, cp, cs, rho = configs.anticline_256_shots(4, nstep=20, n=64)
     best, ms, cand = E.autotune([(s, cp, cs, rho) for s in shots], steps=3)
     n32 = sum(1 for v in E.variants() if not v.fp64 and v.loads == 0)   # TMA-loaded
-    # eleven two-kernel and six dataflow schedules x two prefetch modes for a batch
-    assert cand == n32 * 34
-    assert best.schedule in (0, 1, 2, 3, 4)
+    # eleven two-kernel schedules x two prefetch modes for a batch (the
+    # dataflow schedules are tried for single shots)
+    assert cand == n32 * 22
+    assert best.schedule in (0, 1, 2)
 
 
 CHILD = r"""

@@ -92,3 +92,18 @@ def test_matlab_anticline_restatement():
     # the oil pocket (medium 4) only above k = 80 (1-based)
     k4 = np.nonzero((cp == 3600) & (cs == 1700))[0]
     assert k4.size > 0 and k4.max() < 79
+
+
+@pytest.mark.parametrize("seed", [1000, 1007, 1333])
+def test_serving_request_spec_is_the_same_request(seed):
+    """The device-model form of a serving request has the same grid, time
+    step, source and receivers, and its generated model (host restatement of
+    the device generator) equals the host request's model."""
+    from ela3d_gb300 import configs, media
+
+    p, cp, cs, rho = configs.serving_request(seed, t_end=0.25)
+    q, spec = configs.serving_request_spec(seed, t_end=0.25)
+    assert (p.nx, p.ny, p.nz, p.nstep, p.npml, p.src, p.dt) == (q.nx, q.ny, q.nz, q.nstep, q.npml, q.src, q.dt)
+    assert np.array_equal(p.rec, q.rec)
+    for a, b in zip(media.generate_host(spec, p.nx, p.ny, p.nz), (cp, cs, rho)):
+        assert np.array_equal(a, b)
