@@ -520,10 +520,14 @@ def homogeneous_101(args) -> dict:
                        "1000-step shot, 10 PML cells, Ricker 7 Hz on vz at the centre, 11 receivers",
            "metric": METRIC}
     seis = {}
+    tune = {}
+    if args.c0_schedule >= 0:   # explicit choice for the FP32 shot (profiling comparisons)
+        tune = {"schedule": args.c0_schedule, "chunk": max(args.c0_chunk, 0)}
+        out["tuning"] = tune
     for tag, prec in (("fp32", 0), ("fp64", 1)):
         q = p.with_(precision=prec)
         bpc = bytes_per_cell(p.nx, p.ny, p.nz, p.npml, word=8 if prec else 4)["step"]
-        with E.Plan(q, cp, cs, rho) as pl:   # built-in kernel choice
+        with E.Plan(q, cp, cs, rho, **(tune if prec == 0 else {})) as pl:   # built-in kernel choice
             pl.run(args.warmup)
             ms = pl.run_timed(steps)
             pl.set_kernel_timing(True)
@@ -1051,6 +1055,10 @@ def main():
     ap.add_argument("--c0-steps", type=int, default=400, help="timed steps of the 101^3 cube")
     ap.add_argument("--c0-cpu-steps", type=int, default=100,
                     help="steps of the 101^3 one-core reference CPU samples (about 1-3 s each)")
+    ap.add_argument("--c0-only", action="store_true", help="print only the 101^3 block (profiling runs)")
+    ap.add_argument("--c0-schedule", type=int, default=-1,
+                    help="schedule of the 101^3 FP32 shot (0-4); -1 = built-in choice")
+    ap.add_argument("--c0-chunk", type=int, default=0, help="z-chunk planes with --c0-schedule")
     ap.add_argument("--full", nargs="+", default=[], choices=["batched", "uneven", "serve"],
                     help="instead of the default line: the named batched, uneven and serving configurations at "
                          "their full sizes (64 shots x 2000 steps; 48 grids to t = 2 s; 2000 requests of 2 s)")
@@ -1064,6 +1072,13 @@ def main():
     if args.full:
         if rank == 0:
             run_full(args)
+        return
+    if args.c0_only:
+        if rank == 0:
+            import ela3d_gb300 as E
+
+            E.select_device(local)
+            print(json.dumps({"metric": METRIC, "c0": homogeneous_101(args)}), flush=True)
         return
     if args.impl == "reference":
         run_reference(args, rank, world, local)
