@@ -523,6 +523,9 @@ def homogeneous_101(args) -> dict:
     tune = {}
     if args.c0_schedule >= 0:   # explicit choice for the FP32 shot (profiling comparisons)
         tune = {"schedule": args.c0_schedule, "chunk": max(args.c0_chunk, 0)}
+    if args.c0_variant >= 0:
+        tune["variant"] = args.c0_variant
+    if tune:
         out["tuning"] = tune
     for tag, prec in (("fp32", 0), ("fp64", 1)):
         q = p.with_(precision=prec)
@@ -1059,6 +1062,8 @@ def main():
     ap.add_argument("--c0-schedule", type=int, default=-1,
                     help="schedule of the 101^3 FP32 shot (0-4); -1 = built-in choice")
     ap.add_argument("--c0-chunk", type=int, default=0, help="z-chunk planes with --c0-schedule")
+    ap.add_argument("--c0-variant", type=int, default=-1,
+                    help="kernel variant of the 101^3 FP32 shot (an index of ela3d_gb300.variants()); -1 = built-in")
     ap.add_argument("--full", nargs="+", default=[], choices=["batched", "uneven", "serve"],
                     help="instead of the default line: the named batched, uneven and serving configurations at "
                          "their full sizes (64 shots x 2000 steps; 48 grids to t = 2 s; 2000 requests of 2 s)")

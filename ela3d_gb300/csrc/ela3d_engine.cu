@@ -304,6 +304,17 @@ TuneChoice default_choice(int fp64, int nx, int ny, int nz) {
   if (i == n) i = 0;
   TuneChoice c{i, 1, 10, 0, kPrefetchDefault};
   if (nx > 0 && ny > 0 && nz > 0) {
+    // among the wide tiles of the same shape class (warps, stages), the one
+    // whose width wastes least of a row (101 cells: 112 wide, 90% used,
+    // rather than 128 wide, 79%)
+    auto used = [&](int tx) { return (double)nx / (double)(((nx + tx - 1) / tx) * tx); };
+    const int first = i;
+    for (int j = 0; j < n; ++j)
+      if (j != first && v[j].fp64 == v[first].fp64 && v[j].loads == LOAD_TMA && v[j].threads == v[first].threads &&
+          v[j].ns == v[first].ns && v[j].tx >= 112 && v[j].tx * v[j].ty == v[first].tx * v[first].ty &&
+          used(v[j].tx) > used(v[i].tx) + 0.02)
+        i = j;
+    c.variant = i;
     int dev = 0, sms = 152;
     if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const long long tiles = (long long)((nx + v[i].tx - 1) / v[i].tx) * ((ny + v[i].ty - 1) / v[i].ty);

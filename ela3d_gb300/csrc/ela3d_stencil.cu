@@ -38,6 +38,9 @@ static const Variant kVariants[] = {
     make_variant<float, 64, 14, 4>(),
     make_variant<float, 128, 3, 4>(),
     make_variant<float, 64, 6, 4>(),
+    // 28 threads per row, so a warp spans two rows: covers rows of ~100
+    // cells with less waste than the 128-wide tile (101: 90% against 79%)
+    make_variant<float, 112, 8, 4>(),
     // the 128x7 tile with its stages filled by cp.async instead of TMA (the
     // measured alternative to the tensor-memory-accelerator loads)
     make_variant<float, 128, 7, 4, 4, 0, LOAD_CP_ASYNC>(),

@@ -58,7 +58,7 @@ def test_flow_equals_two_kernels(built, schedule, chunk, lag):
     assert _same(got, want)
 
 
-@pytest.mark.parametrize("tile", [(64, 14), (128, 3), (64, 6), (128, 5)])
+@pytest.mark.parametrize("tile", [(64, 14), (128, 3), (64, 6), (128, 5), (112, 8)])
 def test_flow_tile_variants(built, tile):
     case = _shot(nx=83, ny=61, nz=29, npml=7, nstep=70)
     want = _run(*case, variant=0, schedule=1, chunk=8)
