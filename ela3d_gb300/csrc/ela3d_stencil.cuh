@@ -1103,15 +1103,17 @@ __global__ void __launch_bounds__(Geo<T, TX, TY, NS, CPT, MB>::THREADS, Geo<T, T
 //   velocity (j, tile, step r) reads the stresses of stress (j-1 and j) of
 //                              step r on the tile and its neighbours.
 // Each item, before its loads, waits for those items' completion counters
-// (flags[kind][chunk][tile], one increment per consumer warp at the end of
-// an item: NCW (r + 1) once step r is done); the host orders the list so
-// that every dependency comes earlier (checked there), so the waits always
-// end.  The host's order is a wavefront in z (and, with skew, across
-// steps): a velocity chunk runs right after the stresses it reads were
+// (flags[kind][chunk][tile], NCW added once an item is written: NCW (r + 1)
+// once step r is done); the host orders the list so that every dependency
+// comes earlier (checked there), so the waits always end.  The host places
+// each item soon after the items it waits for (and, with overlapping
+// steps, lets a step start where the previous one is done): a velocity
+// chunk runs right after the stresses it reads were
 // written, while they are still in L2.  Results are bit-identical to the
-// two half-step kernels.  Memory ordering: consumers write, fence the async
-// proxy (the TMA of the reading block), __syncwarp, and one lane releases
-// the counter at gpu scope; the producer acquires the counters (relaxed
+// two half-step kernels.  Memory ordering: consumer warps write, fence the
+// async proxy (the TMA of the reading block), __syncwarp, and arrive (CTA
+// scope) on a shared per-item count; the last warp releases the item's
+// counter at gpu scope; the producer acquires the counters (relaxed
 // loads + fence.acq_rel.gpu), fences the async proxy, arrives on the
 // item's ready barrier and then issues its loads; consumers read global
 // memory for the item only after that barrier.  Every wait is bounded: a wait that passes its limit
@@ -1125,7 +1127,7 @@ struct Flow {
   static constexpr int STAGE = G::S_STAGE > G::V_STAGE ? G::S_STAGE : G::V_STAGE;
   static constexpr int RB = 8;
   static_assert(RB >= NS / 2 + 2, "ready barriers for the items in flight");
-  static constexpr int SMEM = NS * STAGE + 16 * NS + 8 * RB;
+  static constexpr int SMEM = NS * STAGE + 16 * NS + 8 * RB + 4 * RB;
 };
 
 __device__ __forceinline__ int ld_relaxed_gpu(const int *p) {
@@ -1137,6 +1139,12 @@ __device__ __forceinline__ void fence_acq_rel_gpu() { asm volatile("fence.acq_re
 __device__ __forceinline__ void fence_proxy_async_global() { asm volatile("fence.proxy.async.global;" ::: "memory"); }
 __device__ __forceinline__ void red_release_gpu_add(int *p, int v) {
   asm volatile("red.release.gpu.global.add.s32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+// CTA-scope acquire-release add on a shared-memory counter; returns the old value.
+__device__ __forceinline__ int atom_acq_rel_cta_add(int *p, int v) {
+  int old;
+  asm volatile("atom.acq_rel.cta.shared::cta.add.s32 %0, [%1], %2;" : "=r"(old) : "r"(smem_u32(p)), "r"(v) : "memory");
+  return old;
 }
 
 // Lane 0 of the producer: waits until every counter this item depends on
@@ -1201,9 +1209,13 @@ __global__ void __launch_bounds__(Geo<T, TX, TY, NS, CPT, MB>::THREADS, Geo<T, T
   uint64_t *full = reinterpret_cast<uint64_t *>(smem + NS * F::STAGE);
   uint64_t *empty = full + NS;
   uint64_t *ready = empty + NS;   // F::RB barriers, one per item in flight
+  int *arrived = reinterpret_cast<int *>(ready + F::RB);   // F::RB consumer-warp counters
   const int tid = threadIdx.x;
   if (tid == 0)
-    for (int r = 0; r < F::RB; ++r) mbar_init(&ready[r], 1);
+    for (int r = 0; r < F::RB; ++r) {
+      mbar_init(&ready[r], 1);
+      arrived[r] = 0;
+    }
   init_ring<NS, G::NCW, LOAD_TMA>(full, empty);
   const unsigned long long wait_ns = (ctl & CTL_WITHHOLD_LOADS) ? kTestWaitLimitNs : kWaitLimitNs;
 
@@ -1253,6 +1265,7 @@ __global__ void __launch_bounds__(Geo<T, TX, TY, NS, CPT, MB>::THREADS, Geo<T, T
     if (fi.step >= nsteps) continue;
     const ShotDesc<T> &sd = shots[fi.it.shot];
     uint64_t *rb = &ready[idx % F::RB];
+    int *arr = &arrived[idx % F::RB];
     const uint32_t rp = (idx / F::RB) & 1;
     ++idx;
     bool ok;
@@ -1263,13 +1276,17 @@ __global__ void __launch_bounds__(Geo<T, TX, TY, NS, CPT, MB>::THREADS, Geo<T, T
       ok = velocity_item<T, TX, TY, NS, CPT, MB, F::STAGE, true>(sd, fi.it, tick + fi.step, smem, full, empty, n,
                                                                   err, wait_ns, tid, rb, rp);
     if (!ok) return;
-    // this warp's share of the item is written: count it
+    // this warp's share of the item is written: it arrives (CTA scope) on
+    // the item's counter, and the last warp to arrive releases the whole
+    // item at gpu scope -- cumulative over the other warps' writes it has
+    // acquired -- so one gpu-scope fence per item instead of one per warp
     fence_proxy_async_global();
     __syncwarp();
-    if (lane == 0) {
+    if (lane == 0 && atom_acq_rel_cta_add(arr, 1) == G::NCW - 1) {
+      *arr = 0;   // re-armed for item idx + RB (no warp is that far ahead)
       const int txs = (sd.nx + TX - 1) / TX, tys = (sd.ny + TY - 1) / TY;
       int *flag = sd.flow_flags + ((size_t)fi.kind * sd.flow_chunks + fi.chunk) * (txs * tys) + fi.it.tile;
-      red_release_gpu_add(flag, 1);
+      red_release_gpu_add(flag, G::NCW);
     }
     (void)warp;
   }
