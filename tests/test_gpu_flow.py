@@ -151,3 +151,36 @@ def test_flow_timeout_path(built):
             plan.run(10)
         assert e.value.status == 5   # ELA3D_ERR_TIMEOUT
     assert _same(_run(p, cp, cs, rho, variant=0, schedule=3, chunk=8), _run(p, cp, cs, rho, variant=0))
+
+
+@pytest.mark.parametrize("schedule", [3, 4])
+def test_flow_server_mix_equals_alone(built, schedule):
+    """A server on the dataflow kernel (its work list rebuilt whenever
+    requests join or finish) returns every request's seismograms exactly as
+    the request run alone, with late arrivals and a model generated on the
+    device."""
+    import time
+
+    from ela3d_gb300 import Plan, Server, configs
+
+    reqs = [configs.serving_request(s, t_end=0.12, lo=40, hi=96) for s in range(6)]
+    want = []
+    for p, cp, cs, rho in reqs:
+        with Plan(p, cp, cs, rho, variant=0, schedule=1, chunk=8) as plan:
+            plan.run(p.nstep)
+            want.append(plan.seismograms())
+    gp, spec = configs.serving_request_spec(7, t_end=0.12, lo=40, hi=96)
+    with Plan.from_model(gp, spec, variant=0, schedule=1, chunk=8) as plan:
+        plan.run(gp.nstep)
+        want_gen = plan.seismograms()
+    with Server(steps_per_round=29, variant=0, schedule=schedule, chunk=5) as srv:
+        tickets = [srv.submit(*reqs[q]) for q in range(3)]
+        time.sleep(0.05)
+        tickets += [srv.submit(*reqs[q]) for q in range(3, 6)]
+        t_gen = srv.submit_model(gp, spec)
+        for q, t in enumerate(tickets):
+            srv.wait(t)
+            assert np.array_equal(srv.read(t), want[q]), q
+        srv.wait(t_gen)
+        assert np.array_equal(srv.read(t_gen), want_gen)
+        assert srv.stats()["failed"] == 0
