@@ -459,6 +459,7 @@ class Engine final : public EngineBase {
     CK(cudaMemset(d_err_, 0, sizeof(unsigned)));
     CK(cudaMalloc(&d_tick_, sizeof(int)));
     CK(cudaMemset(d_tick_, 0, sizeof(int)));
+    if (const char *e = std::getenv("ELA3D_GRAPH_STEPS")) graph_steps_ = std::max(1, std::atoi(e));
     // ELA3D_PSI_PREFETCH=<bits> overrides the tuned prefetch mode (experiments)
     if (const char *e = std::getenv("ELA3D_PSI_PREFETCH")) prefetch_env_ = std::atoi(e) & (CTL_PF_X | CTL_PF_YZ);
     // ELA3D_GUARD_ZONES=<bytes> (debug): guard zones around every pool array
@@ -931,28 +932,28 @@ class Engine final : public EngineBase {
         }
         continue;
       }
-      // a composition's first kGraphSteps steps run as direct launches; the
+      // a composition's first graph_steps_ steps run as direct launches; the
       // graph is captured only once it has lasted that long (a serving
       // round whose composition never repeats pays for no capture)
-      if (use_graphs_ && !timing_ && inject_ == 0 && !gexec_ && seg >= kGraphSteps &&
-          steps_on_schedule_ < kGraphSteps) {
-        for (int d = std::min(seg, kGraphSteps - steps_on_schedule_); d > 0; --d, --seg) {
+      if (use_graphs_ && !timing_ && inject_ == 0 && !gexec_ && seg >= graph_steps_ &&
+          steps_on_schedule_ < graph_steps_) {
+        for (int d = std::min(seg, graph_steps_ - steps_on_schedule_); d > 0; --d, --seg) {
           ela3d_status st = launch_step(tick_ + 1, nullptr);
           if (st != ELA3D_OK) return st;
           ++tick_;
           ++steps_on_schedule_;
         }
       }
-      const bool graphs = use_graphs_ && !timing_ && inject_ == 0 && seg >= kGraphSteps;
+      const bool graphs = use_graphs_ && !timing_ && inject_ == 0 && seg >= graph_steps_;
       if (graphs) {
         ela3d_status st = ensure_graph();
         if (st != ELA3D_OK) return st;
         CK(launch_tick_set(d_tick_, tick_ + 1, stream_));
-        while (seg >= kGraphSteps) {
+        while (seg >= graph_steps_) {
           CK(cudaGraphLaunch(gexec_, stream_));
-          tick_ += kGraphSteps;
-          seg -= kGraphSteps;
-          launches_ += (int64_t)kGraphSteps * (2 + (any_explosive_ ? 1 : 0));
+          tick_ += graph_steps_;
+          seg -= graph_steps_;
+          launches_ += (int64_t)graph_steps_ * (2 + (any_explosive_ ? 1 : 0));
         }
       }
       for (; seg > 0; --seg) {
@@ -1149,20 +1150,20 @@ class Engine final : public EngineBase {
     gexec_ = nullptr;
   }
 
-  // A replayable graph of kGraphSteps steps reading the step from d_tick_
+  // A replayable graph of graph_steps_ steps reading the step from d_tick_
   // and advancing it at the end.
   ela3d_status ensure_graph() {
     if (gexec_) return ELA3D_OK;
     CK(cudaStreamBeginCapture(stream_, cudaStreamCaptureModeThreadLocal));
     capturing_ = true;
     ela3d_status st = ELA3D_OK;
-    for (int i = 0; i < kGraphSteps && st == ELA3D_OK; ++i) st = launch_step(i, d_tick_);
+    for (int i = 0; i < graph_steps_ && st == ELA3D_OK; ++i) st = launch_step(i, d_tick_);
     cudaError_t e = cudaSuccess;
-    if (st == ELA3D_OK) e = launch_tick_add(d_tick_, kGraphSteps, stream_);
+    if (st == ELA3D_OK) e = launch_tick_add(d_tick_, graph_steps_, stream_);
     cudaGraph_t g = nullptr;
     cudaError_t e2 = cudaStreamEndCapture(stream_, &g);
     capturing_ = false;
-    launches_ -= (int64_t)kGraphSteps * (2 + (any_explosive_ ? 1 : 0));  // counted when replayed
+    launches_ -= (int64_t)graph_steps_ * (2 + (any_explosive_ ? 1 : 0));  // counted when replayed
     if (st != ELA3D_OK) { if (g) cudaGraphDestroy(g); return st; }
     if (e != cudaSuccess || e2 != cudaSuccess) {
       if (g) cudaGraphDestroy(g);
@@ -1579,6 +1580,9 @@ class Engine final : public EngineBase {
   int64_t launches_ = 0;
   uint64_t next_key_ = 1;
   static constexpr int kGraphSteps = 50;
+  // steps per replayed graph; ELA3D_GRAPH_STEPS=<n> overrides it (the
+  // measurement of one graph per whole run against replays of 50 steps)
+  int graph_steps_ = kGraphSteps;
   bool timing_ = false;
   std::vector<Ev> pending_;
   std::vector<cudaEvent_t> free_events_;
