@@ -423,7 +423,22 @@ __device__ __forceinline__ bool stress_item(const ShotDesc<T> &sd, const Item &i
   const int syl = sl + WW;                 // vy box (origin x0-H, y0-1): own row is ty+1
   const int sc = ty * TX + tx * V;         // centre boxes
 
-  for (int k = item.k0; k < item.k1; ++k) {
+  // the update ranges (simpelmodel.cpp:378-498) as per-cell bits, set once
+  // per work item; the normal stresses also need k >= 1 (applied per plane)
+  unsigned mbits = 0;
+#pragma unroll
+  for (int e = 0; e < V; ++e) {
+    const int x = xg + e;
+    mbits |= ((y >= 1) && (x <= nx - 2) ? 1u : 0u) << e;                   // normal: j >= 2, i <= NX-1
+    mbits |= ((y <= ny - 2) && (x >= 1) && (x <= nx - 1) ? 1u : 0u) << (8 + e);   // sigma_xy
+    mbits |= ((x >= 1) && (x <= nx - 1) ? 1u : 0u) << (16 + e);            // sigma_xz
+    mbits |= ((y <= ny - 2) && (x <= nx - 1) ? 1u : 0u) << (24 + e);       // sigma_yz
+  }
+  T *gx = psi_x + ((long long)item.k0 * ny + y) * xw + xs;
+  T *gy = psi_y + ((long long)item.k0 * yw + ys) * px + xg;
+  const long long dgx = (long long)ny * xw, dgy = (long long)yw * px;
+  long long g = (long long)item.k0 * plane + rowoff;
+  for (int k = item.k0; k < item.k1; ++k, gx += dgx, gy += dgy, g += plane) {
     // memory variables and z profile first: their latency overlaps the wait
     const bool plane_z = k < zl || k >= zr;       // the plane lies in the z slab
     const bool in_z = live && plane_z;
@@ -434,8 +449,6 @@ __device__ __forceinline__ bool stress_item(const ShotDesc<T> &sd, const Item &i
       azh = prof_z[PR_AH * nz + k]; bzh = prof_z[PR_BH * nz + k]; ikzh = prof_z[PR_IKH * nz + k];
     }
     T px0[V], px1[V], px2[V], py0[V], py1[V], py2[V], pz0[V], pz1[V], pz2[V];
-    T *gx = psi_x + ((long long)k * ny + y) * xw + xs;
-    T *gy = psi_y + ((long long)k * yw + ys) * px + xg;
     T *gz = psi_z + ((long long)zs * ny + y) * px + xg;
     if (in_x) {
       ld_vec_rw(gx + PSI_S0 * psx, px0);
@@ -513,8 +526,8 @@ __device__ __forceinline__ bool stress_item(const ShotDesc<T> &sd, const Item &i
       if (last) mbar_arrive(&empty[s1]);
     }
 
-    const bool yN = (y >= 1) && (k >= 1);   // normal stresses: j >= 2, k >= 2 (1-based)
-    const bool yXY = (y <= ny - 2);         // sigma_xy and sigma_yz: j <= NY-1
+    // this plane's update masks: bit e of byte c = component c of cell e
+    const unsigned mk = k >= 1 ? mbits : (mbits & 0xffffff00u);
     // The y- and z-direction C-PML terms are evaluated only for rows /
     // planes inside the slabs (elsewhere a = 0 and 1/K = 1 and the terms
     // are exact no-ops).  Memory variables are updated whether or not the
@@ -532,7 +545,7 @@ __device__ __forceinline__ bool stress_item(const ShotDesc<T> &sd, const Item &i
 
         // normal stresses, simpelmodel.cpp:378-413
         {
-          const bool m = yN && (x <= nx - 2);
+          const bool m = (mk >> (0 + e)) & 1u;
           const T vp = cp_c[e], vs = cs_c[e], rhos = rho_c[e];
           const T lambda = rhos * (vp * vp - T(2) * vs * vs);
           const T l2m = rhos * vp * vp;
@@ -561,7 +574,7 @@ __device__ __forceinline__ bool stress_item(const ShotDesc<T> &sd, const Item &i
         }
         // sigma_xy, :416-442
         {
-          const bool m = yXY && (x >= 1) && (x <= nx - 1);
+          const bool m = (mk >> (8 + e)) & 1u;
           const T vs = (cs_xm + cs_yp[e]) / T(2);
           const T rhos = (rho_xm + rho_yp[e]) / T(2);
           const T DT_mu = dt * (rhos * vs * vs);
@@ -579,7 +592,7 @@ __device__ __forceinline__ bool stress_item(const ShotDesc<T> &sd, const Item &i
         }
         // sigma_xz, :445-471 (z+1 of plane nz-1 is the zero plane)
         {
-          const bool m = (x >= 1) && (x <= nx - 1);
+          const bool m = (mk >> (16 + e)) & 1u;
           const T vs = (cs_xm + cs_zp[e]) / T(2);
           const T rhos = (rho_xm + rho_zp[e]) / T(2);
           const T DT_mu = dt * (rhos * vs * vs);
@@ -597,7 +610,7 @@ __device__ __forceinline__ bool stress_item(const ShotDesc<T> &sd, const Item &i
         }
         // sigma_yz, :473-498
         {
-          const bool m = yXY && (x <= nx - 1);
+          const bool m = (mk >> (24 + e)) & 1u;
           const T vs = (cs_yp[e] + cs_zp[e]) / T(2);
           const T rhos = (rho_yp[e] + rho_zp[e]) / T(2);
           const T DT_mu = dt * (rhos * vs * vs);
@@ -627,7 +640,6 @@ __device__ __forceinline__ bool stress_item(const ShotDesc<T> &sd, const Item &i
     }
 
     if (live) {
-      const long long g = (long long)k * plane + rowoff;
       st_vec(f3 + g, sxx);
       st_vec(f4 + g, syy);
       st_vec(f5 + g, szz);
@@ -735,7 +747,21 @@ __device__ __forceinline__ bool velocity_item(const ShotDesc<T> &sd, const Item 
   const int sc = ty * TX + tx * V;          // syy box (origin x0, y0) / centre boxes
   const int sc1 = (ty + 1) * TX + tx * V;   // syz box (origin x0, y0-1)
 
-  for (int k = item.k0; k < item.k1; ++k) {
+  // the update ranges (simpelmodel.cpp:502-590) as per-cell bits, set once
+  // per work item; the plane conditions are applied per plane
+  unsigned mbits = 0;
+#pragma unroll
+  for (int e = 0; e < V; ++e) {
+    const int x = xg + e;
+    mbits |= ((y >= 1) && (x >= 1) && (x <= nx - 1) ? 1u : 0u) << e;        // vx (with k >= 1)
+    mbits |= ((y <= ny - 2) && (x <= nx - 2) ? 1u : 0u) << (8 + e);         // vy (with k >= 1)
+    mbits |= ((y >= 1) && (x <= nx - 2) ? 1u : 0u) << (16 + e);             // vz (with k <= nz-2)
+  }
+  T *gx = psi_x + ((long long)item.k0 * ny + y) * xw + xs;
+  T *gy = psi_y + ((long long)item.k0 * yw + ys) * px + xg;
+  const long long dgx = (long long)ny * xw, dgy = (long long)yw * px;
+  long long g = (long long)item.k0 * plane + rowoff;
+  for (int k = item.k0; k < item.k1; ++k, gx += dgx, gy += dgy, g += plane) {
     const bool plane_z = k < zl || k >= zr;       // the plane lies in the z slab
     const bool in_z = live && plane_z;
     const int zs = k < zl ? k : zl + (k - zr);
@@ -745,8 +771,6 @@ __device__ __forceinline__ bool velocity_item(const ShotDesc<T> &sd, const Item 
       azh = prof_z[PR_AH * nz + k]; bzh = prof_z[PR_BH * nz + k]; ikzh = prof_z[PR_IKH * nz + k];
     }
     T px0[V], px1[V], px2[V], py0[V], py1[V], py2[V], pz0[V], pz1[V], pz2[V];
-    T *gx = psi_x + ((long long)k * ny + y) * xw + xs;
-    T *gy = psi_y + ((long long)k * yw + ys) * px + xg;
     T *gz = psi_z + ((long long)zs * ny + y) * px + xg;
     if (in_x) {
       ld_vec_rw(gx + PSI_V0 * psx, px0);
@@ -822,10 +846,8 @@ __device__ __forceinline__ bool velocity_item(const ShotDesc<T> &sd, const Item 
       if (last) mbar_arrive(&empty[s1]);
     }
 
-    const bool mvx_yz = (y >= 1) && (k >= 1);
-    const bool mvy_yz = (y <= ny - 2) && (k >= 1);
-    const bool mvz_yz = (y >= 1) && (k <= nz - 2);
-    T rbx[V], rby[V], rbz[V];   // averaged densities (reused by the source)
+    // this plane's update masks: bit e of byte c = component c of cell e
+    const unsigned mk = (k >= 1 ? (mbits & 0x00ffffu) : 0u) | (k <= nz - 2 ? (mbits & 0xff0000u) : 0u);
     // y/z C-PML terms only inside the slabs; memory variables updated
     // whether or not the cell's velocity is (as in the stress half-step)
     auto compute = [&](auto PY, auto PZ) {
@@ -839,9 +861,8 @@ __device__ __forceinline__ bool velocity_item(const ShotDesc<T> &sd, const Item 
         const T sxz_xp = (e < V - 1) ? sxz_c[e + 1] : sxz_e;
         // vx, simpelmodel.cpp:502-530
         {
-          const bool m = mvx_yz && (x >= 1) && (x <= nx - 1);
+          const bool m = (mk >> (0 + e)) & 1u;
           const T rhos = (rho_c[e] + rho_xm) / T(2);
-          rbx[e] = rhos;
           const T DT_over_rho = div_fast(dt, rhos);
           T d1 = (sxx_c[e] - sxx_xm) * idx;
           T d2 = (sxy_c[e] - sxy_ym[e]) * idy;
@@ -863,9 +884,8 @@ __device__ __forceinline__ bool velocity_item(const ShotDesc<T> &sd, const Item 
         }
         // vy, :532-559
         {
-          const bool m = mvy_yz && (x <= nx - 2);
+          const bool m = (mk >> (8 + e)) & 1u;
           const T rhos = (rho_c[e] + rho_yp[e]) / T(2);
-          rby[e] = rhos;
           const T DT_over_rho = div_fast(dt, rhos);
           T d1 = (sxy_xp - sxy_c[e]) * idx;
           T d2 = (syy_yp[e] - syy_c[e]) * idy;
@@ -887,9 +907,8 @@ __device__ __forceinline__ bool velocity_item(const ShotDesc<T> &sd, const Item 
         }
         // vz, :563-590
         {
-          const bool m = mvz_yz && (x <= nx - 2);
+          const bool m = (mk >> (16 + e)) & 1u;
           const T rhos = (rho_c[e] + rho_zp[e]) / T(2);
-          rbz[e] = rhos;
           const T DT_over_rho = div_fast(dt, rhos);
           T d1 = (sxz_xp - sxz_c[e]) * idx;
           T d2 = (syz_c[e] - syz_ym[e]) * idy;
@@ -954,15 +973,22 @@ __device__ __forceinline__ bool velocity_item(const ShotDesc<T> &sd, const Item 
       if (src_row && k == sd.src_k) {
         const T s = sd.stf[it_step - 1];
         const int se = sd.src_i - xg;
+        // the averaged densities at the source cell, from the model itself
+        // (out-of-grid neighbours are zero, as in the stage boxes)
+        const long long gs = (long long)k * plane + rowoff + se;
+        const T r0 = sd.rho[gs];
+        const T rxs = (r0 + (sd.src_i >= 1 ? sd.rho[gs - 1] : T(0))) / T(2);
+        const T rys = (r0 + (y + 1 < ny ? sd.rho[gs + px] : T(0))) / T(2);
+        const T rzs = (r0 + (k + 1 < nz ? sd.rho[gs + plane] : T(0))) / T(2);
         const bool wx = sd.src_w[0] != T(0), wy = sd.src_w[1] != T(0), wz = sd.src_w[2] != T(0);
         const T fx = sd.src_w[0] * s, fy = sd.src_w[1] * s, fz = sd.src_w[2] * s;
         T tvx = vx[0], tvy = vy[0], tvz = vz[0];
 #pragma unroll
         for (int c = 0; c < V; ++c) {
           const bool hit = (c == se);
-          vx[c] = (hit && wx) ? vx[c] + fx * dt / rbx[c] : vx[c];
-          vy[c] = (hit && wy) ? vy[c] + fy * dt / rby[c] : vy[c];
-          vz[c] = (hit && wz) ? vz[c] + fz * dt / rbz[c] : vz[c];
+          vx[c] = (hit && wx) ? vx[c] + fx * dt / rxs : vx[c];
+          vy[c] = (hit && wy) ? vy[c] + fy * dt / rys : vy[c];
+          vz[c] = (hit && wz) ? vz[c] + fz * dt / rzs : vz[c];
           tvx = hit ? vx[c] : tvx;
           tvy = hit ? vy[c] : tvy;
           tvz = hit ? vz[c] : tvz;
@@ -973,7 +999,6 @@ __device__ __forceinline__ bool velocity_item(const ShotDesc<T> &sd, const Item 
         sd.src_trace[ns + it_step] = tvy;
         sd.src_trace[2 * ns + it_step] = tvz;
       }
-      const long long g = (long long)k * plane + rowoff;
       st_vec(f0 + g, vx);
       st_vec(f1 + g, vy);
       st_vec(f2 + g, vz);
