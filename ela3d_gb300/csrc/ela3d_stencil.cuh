@@ -317,13 +317,15 @@ __device__ __forceinline__ void velocity_issue(const ShotDesc<T> *__restrict__ s
   for (int c = 0; c < 3; ++c) tma_load_3d(st + G::V_V + c * G::SC, &m[7 + c], x0, y0, k, bar);
 }
 
-// Waits for the stages of loads n and n+1 (planes k and k+1).  False when a
-// wait passed its limit; the caller records the timeout and returns.
+// Waits for the stages of loads n and n+1 (planes k and k+1); load n was
+// already waited for as the previous plane's k+1 unless k is the first plane
+// of its work item.  False when a wait passed its limit; the caller records
+// the timeout and returns.
 template <int NS>
-__device__ __forceinline__ bool wait_planes(uint64_t *full, unsigned n, unsigned long long wait_ns, unsigned *err,
-                                            int lane) {
+__device__ __forceinline__ bool wait_planes(uint64_t *full, unsigned n, bool first, unsigned long long wait_ns,
+                                            unsigned *err, int lane) {
   const int s0 = (int)(n % NS), s1 = (int)((n + 1) % NS);
-  bool ok = mbar_wait_bounded(&full[s0], (uint32_t)((n / NS) & 1), wait_ns);
+  bool ok = !first || mbar_wait_bounded(&full[s0], (uint32_t)((n / NS) & 1), wait_ns);
   ok = ok && mbar_wait_bounded(&full[s1], (uint32_t)(((n + 1) / NS) & 1), wait_ns);
   if (__any_sync(0xffffffffu, !ok)) {
     if (lane == 0) atomicOr(err, DEV_ERR_TIMEOUT);
@@ -475,7 +477,7 @@ __device__ __forceinline__ bool stress_item(const ShotDesc<T> &sd, const Item &i
       for (int e = 0; e < V; ++e) pz0[e] = pz1[e] = pz2[e] = T(0);
     }
 
-    if (!wait_planes<NS>(full, n, wait_ns, err, lane)) return false;
+    if (!wait_planes<NS>(full, n, k == item.k0, wait_ns, err, lane)) return false;
     const int s0 = (int)(n % NS), s1 = (int)((n + 1) % NS);
     const unsigned char *cur = smem + s0 * STAGE;
     const unsigned char *nxt = smem + s1 * STAGE;
@@ -803,7 +805,7 @@ __device__ __forceinline__ bool velocity_item(const ShotDesc<T> &sd, const Item 
       rhi = rec_plane[k + 1];
     }
 
-    if (!wait_planes<NS>(full, n, wait_ns, err, lane)) return false;
+    if (!wait_planes<NS>(full, n, k == item.k0, wait_ns, err, lane)) return false;
     const int s0 = (int)(n % NS), s1 = (int)((n + 1) % NS);
     const unsigned char *cur = smem + s0 * STAGE;
     const unsigned char *nxt = smem + s1 * STAGE;
