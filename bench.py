@@ -600,10 +600,12 @@ def batched_shots(args, single_value: float, single_wall_value: float | None = N
     tune = {"schedule": args.batch_schedule, "chunk": args.batch_chunk}
     tune_info = {"source": "command line"}
     if not args.no_autotune:
-        # tuned on 8 of the shots (the per-cell speed is what differs)
-        best, _, cand = E.autotune([(p, cp, cs, rho) for p in shots[:8]], steps=5)
+        # tuned on 16 of the shots over 10 steps: with 8 shots and 5 steps the
+        # pick varied between runs and at times chose a tile 3% slower for
+        # the whole batch
+        best, _, cand = E.autotune([(p, cp, cs, rho) for p in shots[:16]], steps=10)
         tune = best.as_dict()
-        tune_info = {"source": "ela3d_autotune on 8 of the shots", "candidates": cand, **tune}
+        tune_info = {"source": "ela3d_autotune on 16 of the shots, 10 steps", "candidates": cand, **tune}
     t0 = time.perf_counter()
     with E.Batch([(p, cp, cs, rho) for p in shots], **tune) as b:
         t_create = time.perf_counter() - t0
