@@ -99,7 +99,8 @@ class PlanInfo(ctypes.Structure):
 class VariantInfo(ctypes.Structure):
     _fields_ = [("fp64", ctypes.c_int32), ("tile_x", ctypes.c_int32), ("tile_y", ctypes.c_int32),
                 ("stages", ctypes.c_int32), ("threads", ctypes.c_int32), ("stress_smem", ctypes.c_int32),
-                ("velocity_smem", ctypes.c_int32), ("loads", ctypes.c_int32)]
+                ("velocity_smem", ctypes.c_int32), ("loads", ctypes.c_int32),
+                ("velocity_stages", ctypes.c_int32)]
 
 
 class Tuning(ctypes.Structure):

@@ -124,6 +124,7 @@ ela3d_status ela3d_variant_get(int32_t index, ela3d_variant_info *out) {
   out->stress_smem = v[index].stress_smem;
   out->velocity_smem = v[index].vel_smem;
   out->loads = v[index].loads;
+  out->velocity_stages = v[index].ns_vel;
   return ELA3D_OK;
 }
 

@@ -12,7 +12,8 @@ namespace ela3d {
 // One compiled instance of the two stencil kernels.
 struct Variant {
   int fp64;             // 0 float, 1 double
-  int tx, ty, ns;       // tile and pipeline depth
+  int tx, ty, ns;       // tile and pipeline depth (stress kernel, dataflow kernel)
+  int ns_vel;           // pipeline depth of the velocity kernel
   int threads;          // threads per block
   int stress_smem, vel_smem;  // dynamic shared memory bytes
   int halo;             // x halo (elements) of the wide boxes

@@ -235,11 +235,13 @@ ela3d_status ela3d_plan_check_guards(ela3d_plan *plan);
  * tile and shared-memory pipeline depth.  No counterpart in the reference
  * (its kernels use fixed 10^3 thread blocks, cudazerocopy.cu:1361-1369). */
 typedef struct ela3d_variant_info {
-    int32_t fp64, tile_x, tile_y, stages, threads;
+    int32_t fp64, tile_x, tile_y, stages, threads;   /* stages: of the stress
+                                                        (and dataflow) kernel's ring */
     int32_t stress_smem, velocity_smem;
     int32_t loads;   /* 0: stages filled by TMA tiled loads; 1: by cp.async
                         copies of the whole loading warp (a measured
                         alternative, not a default) */
+    int32_t velocity_stages;   /* stages of the velocity kernel's ring */
 } ela3d_variant_info;
 
 /* Work schedule: kind 0 = equal contiguous share of (tile, plane) units per
