@@ -56,6 +56,8 @@ SIGNATURES = [
     ("ela3d_plan_get_profiles", _c.c_int, [_P, _c.c_int32, _c.c_void_p]),
     ("ela3d_plan_check_guards", _c.c_int, [_P]),
     ("ela3d_select_device", _c.c_int, [_c.c_int32]),
+    ("ela3d_host_alloc", _c.c_int, [_c.c_size_t, _c.POINTER(_P)]),
+    ("ela3d_host_free", _c.c_int, [_P]),
     ("ela3d_run_timed", _c.c_int, [_P, _c.c_int32, _c.POINTER(_c.c_double)]),
     ("ela3d_slab_extent", _c.c_int, [_P, _P, _c.c_int32, _c.POINTER(_c.c_int32), _c.POINTER(_c.c_int32)]),
     ("ela3d_schedule_build", _c.c_int, [_c.c_int32] * 8 + [_c.POINTER(_c.c_int32), _c.POINTER(_c.c_int32), _P, _P]),
@@ -228,6 +230,44 @@ def select_device(ordinal: int) -> None:
     _check(load_library().ela3d_select_device(ordinal), "ela3d_select_device")
 
 
+class _HostBuffer:
+    """Owner of one page-locked allocation; freed when the last array view
+    of it is collected."""
+
+    def __init__(self, nbytes: int):
+        self._lib = load_library()
+        self.ptr = ctypes.c_void_p()
+        _check(self._lib.ela3d_host_alloc(nbytes, ctypes.byref(self.ptr)), "ela3d_host_alloc")
+        self.nbytes = nbytes
+
+    def __del__(self):
+        if getattr(self, "ptr", None) and self.ptr.value:
+            self._lib.ela3d_host_free(self.ptr)
+            self.ptr = ctypes.c_void_p()
+
+
+def pinned_empty(shape, dtype=np.float32) -> np.ndarray:
+    """A numpy array in page-locked host memory (ela3d_host_alloc): model
+    arrays and read-back buffers in it copy at the link's full rate."""
+    dtype = np.dtype(dtype)
+    count = int(np.prod(shape)) if np.ndim(shape) else int(shape)
+    owner = _HostBuffer(max(1, count * dtype.itemsize))
+    raw = (ctypes.c_char * owner.nbytes).from_address(owner.ptr.value)
+    arr = np.frombuffer(raw, dtype=dtype, count=count).reshape(shape)
+    arr.flags.writeable = True
+    # the ctypes buffer keeps the owner alive as long as any view exists
+    raw._owner = owner
+    return arr
+
+
+def pinned_copy(a: np.ndarray, dtype=None) -> np.ndarray:
+    """A page-locked copy of a."""
+    a = np.asarray(a, dtype=dtype)
+    out = pinned_empty(a.shape, a.dtype)
+    out[...] = a
+    return out
+
+
 def _check(st: int, where: str) -> None:
     if st != 0:
         raise Ela3dError(st, where)
@@ -294,9 +334,15 @@ class Plan:
     def sync(self) -> None:
         _check(self._lib.ela3d_sync(self._h), "ela3d_sync")
 
-    def seismograms(self, fp64: bool = False) -> np.ndarray:
+    def seismograms(self, fp64: bool = False, out: np.ndarray | None = None) -> np.ndarray:
+        """[nrec, 3, nsamp] receiver traces; `out` (C-contiguous, of that
+        shape and float32 / float64) receives them instead of a new array."""
         p = self.params
-        out = np.zeros((p.nrec, 3, p.nsamp), np.float64 if fp64 else np.float32)
+        dt = np.float64 if fp64 else np.float32
+        if out is None:
+            out = np.zeros((p.nrec, 3, p.nsamp), dt)
+        elif out.shape != (p.nrec, 3, p.nsamp) or out.dtype != dt or not out.flags.c_contiguous:
+            raise ValueError("out must be a C-contiguous [nrec, 3, nsamp] array of the requested precision")
         if out.size:
             fn = self._lib.ela3d_get_seismograms_f64 if fp64 else self._lib.ela3d_get_seismograms
             _check(fn(self._h, _ptr(out)), "ela3d_get_seismograms")

@@ -257,6 +257,17 @@ ela3d_status ela3d_select_device(int32_t ordinal) {
   return status_from_cuda(cudaSetDevice(ordinal), "cudaSetDevice");
 }
 
+ela3d_status ela3d_host_alloc(size_t bytes, void **out) {
+  if (!out || bytes == 0) return ELA3D_ERR_INVALID_ARG;
+  *out = nullptr;
+  return status_from_cuda(cudaHostAlloc(out, bytes, cudaHostAllocDefault), "cudaHostAlloc");
+}
+
+ela3d_status ela3d_host_free(void *ptr) {
+  if (!ptr) return ELA3D_OK;
+  return status_from_cuda(cudaFreeHost(ptr), "cudaFreeHost");
+}
+
 ela3d_status ela3d_run_timed(ela3d_plan *plan, int32_t nsteps, double *ms) {
   if (!plan || nsteps < 0) return ELA3D_ERR_INVALID_ARG;
   return plan->eng->run_timed(nsteps, ms);

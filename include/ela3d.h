@@ -21,6 +21,7 @@
 #ifndef ELA3D_H
 #define ELA3D_H
 
+#include <stddef.h>
 #include <stdint.h>
 
 #ifdef __cplusplus
@@ -130,6 +131,14 @@ ela3d_status ela3d_params_default(ela3d_params *p);
 /* Makes device `ordinal` current for this thread's later calls (the
  * reference always uses device 0; one process per GPU selects its own). */
 ela3d_status ela3d_select_device(int32_t ordinal);
+
+/* Page-locked host buffers: model arrays and read-back buffers in them copy
+ * to and from the device at the link's full rate (pageable memory goes
+ * through a staging copy).  No counterpart: the reference's GPU program
+ * copies its model from malloc'd arrays (cudazerocopy.cu:539-541,631-633).
+ * ela3d_host_free takes only pointers from ela3d_host_alloc (or NULL). */
+ela3d_status ela3d_host_alloc(size_t bytes, void **out);
+ela3d_status ela3d_host_free(void *ptr);
 
 /* ---- single shot -------------------------------------------------------- */
 /* Replaces main()'s setup: allocations and zero fill (simpelmodel.cpp:80-140),
