@@ -57,6 +57,7 @@ SIGNATURES = [
     ("ela3d_plan_check_guards", _c.c_int, [_P]),
     ("ela3d_select_device", _c.c_int, [_c.c_int32]),
     ("ela3d_host_alloc", _c.c_int, [_c.c_size_t, _c.POINTER(_P)]),
+    ("ela3d_builtin_tuning", _c.c_int, [_c.POINTER(CParams), _P]),
     ("ela3d_host_free", _c.c_int, [_P]),
     ("ela3d_run_timed", _c.c_int, [_P, _c.c_int32, _c.POINTER(_c.c_double)]),
     ("ela3d_slab_extent", _c.c_int, [_P, _P, _c.c_int32, _c.POINTER(_c.c_int32), _c.POINTER(_c.c_int32)]),
@@ -224,6 +225,15 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
         fn.argtypes = args
     _LIB = lib
     return lib
+
+
+def builtin_tuning(p) -> "Tuning":
+    """The built-in kernel choice for a single shot with parameters p
+    (ela3d_builtin_tuning; host only)."""
+    c, _rec = p.to_c()
+    t = Tuning()
+    _check(load_library().ela3d_builtin_tuning(ctypes.byref(c), ctypes.addressof(t)), "ela3d_builtin_tuning")
+    return t
 
 
 def select_device(ordinal: int) -> None:

@@ -136,7 +136,8 @@ static TuneChoice resolve_tuning(const std::vector<ela3d_params> &ps, const floa
   const ela3d_params &p = ps[0];
   // (the size-aware default applies to single shots; many shots give
   // round-robin chunks enough to go around)
-  TuneChoice c = ps.size() == 1 ? default_choice(p.precision == ELA3D_FP64, p.nx, p.ny, p.nz)
+  TuneChoice c = ps.size() == 1 ? default_choice(p.precision == ELA3D_FP64, p.nx, p.ny, p.nz,
+                                                 p.src_kind == ELA3D_SRC_EXPLOSIVE)
                                 : default_choice(p.precision == ELA3D_FP64, 0, 0, 0);
   const bool explicit_variant = t && t->variant >= 0;
   if (!explicit_variant) {
@@ -411,6 +412,19 @@ ela3d_status ela3d_slab_extent(const double *a_full, const double *a_half, int32
   slab_extent(a_full, a_half, n, &l, &h);
   *lo = l;
   *hi = h;
+  return ELA3D_OK;
+}
+
+ela3d_status ela3d_builtin_tuning(const ela3d_params *p, ela3d_tuning *out) {
+  if (!p || !out) return ELA3D_ERR_INVALID_ARG;
+  const TuneChoice c = default_choice(p->precision == ELA3D_FP64, p->nx, p->ny, p->nz,
+                                      p->src_kind == ELA3D_SRC_EXPLOSIVE);
+  out->variant = c.variant;
+  out->schedule = c.kind;
+  out->chunk = c.chunk;
+  out->blocks_per_sm = c.blocks_per_sm;
+  out->prefetch = c.prefetch;
+  out->lag = c.lag;
   return ELA3D_OK;
 }
 

@@ -291,7 +291,7 @@ bool build_flow_schedule(const std::vector<FlowShape> &shots, int tx, int ty, in
   return true;
 }
 
-TuneChoice default_choice(int fp64, int nx, int ny, int nz) {
+TuneChoice default_choice(int fp64, int nx, int ny, int nz, bool explosive) {
   int n = 0;
   const Variant *v = variants(&n);
   // first variant of the precision (the list is ordered best first for
@@ -330,19 +330,29 @@ TuneChoice default_choice(int fp64, int nx, int ny, int nz) {
       c.chunk = std::max(10, ch);
     }
     const long long chunks = tiles * ((nz + c.chunk - 1) / c.chunk);
-    if (chunks < 8ll * std::max(1, sms)) c.kind = 0;
+    if (chunks < 4ll * std::max(1, sms)) c.kind = 0;
     // a shot whose twelve arrays fit in L2 gains nothing from bringing its
     // y/z-slab memory variables into L2 ahead of use
     const double bytes = 12.0 * nx * ny * nz * (fp64 ? 8.0 : 4.0);
     if (bytes < 96.0 * (1 << 20)) c.prefetch = CTL_PF_X;
-    // FP32 grids whose arrays are within about twice the L2 run faster in
-    // the dataflow kernel with overlapping steps (measured: 101^3 +15% with
-    // 6-plane chunks, 128^3 +9% with 8-plane chunks; at 256^3 the two
-    // half-step kernels stay ahead)
-    if (!fp64 && v[i].flow && bytes < 256.0 * (1 << 20)) {
-      c.kind = kScheduleFlowOverlap;
-      c.chunk = bytes < 64.0 * (1 << 20) ? 6 : 8;
-      c.lag = 0;
+    // FP32 shots run faster in the dataflow kernel with overlapping steps
+    // when the half-step's work items (tile columns cut into z-chunks) number
+    // about 1.5 per block with at least three chunks per column: no launch
+    // boundaries, no tail of a half-step, and for grids near the L2 size the
+    // exchange between the half-steps through L2.  Measured (Gcell/s,
+    // dataflow against the best two-kernel chunk): 101^3 32.2 vs 26.4,
+    // 128^3 29.7 vs 22.5, 160^3 30.8 vs 25.9, 192^3 38.9 vs 34.1, 224^3
+    // 42.6 vs 40.8, 256^3 45.6 vs 44.5, 288^3 42.0 vs 41.2; at 320^3 (two
+    // chunks per column) the two kernels stay ahead, 43.5 vs 42.5.  An
+    // explosive source injects between the half-steps, so it keeps the
+    // two kernels.
+    if (!fp64 && !explosive && v[i].flow) {
+      const long long per_col = (3ll * sms / 2 + tiles - 1) / tiles;   // z-chunks per tile column
+      if (per_col >= 3) {
+        c.kind = kScheduleFlowOverlap;
+        c.chunk = std::max(4, (int)((nz + per_col - 1) / per_col));
+        c.lag = 0;
+      }
     }
   }
   return c;
@@ -801,7 +811,9 @@ class Engine final : public EngineBase {
     if (shots_.empty() && !choice) BAD("no shots");
     int nv = 0;
     const Variant *vs = variants(&nv);
-    TuneChoice c = choice ? *choice : default_choice(sizeof(T) == 8, shots_[0]->p.nx, shots_[0]->p.ny, shots_[0]->p.nz);
+    TuneChoice c = choice ? *choice
+                          : default_choice(sizeof(T) == 8, shots_[0]->p.nx, shots_[0]->p.ny, shots_[0]->p.nz,
+                                           shots_[0]->p.src_kind == ELA3D_SRC_EXPLOSIVE);
     if (c.variant < 0 || c.variant >= nv || vs[c.variant].fp64 != (sizeof(T) == 8)) BAD("bad kernel variant");
     var_ = &vs[c.variant];
     choice_ = c;
@@ -1087,10 +1099,13 @@ class Engine final : public EngineBase {
     std::vector<int> off, nch;
     int nflags = 0;
     std::string why;
-    // gap: by default about one round of the grid, so an item is claimed
-    // when the items it waits for have finished while their results are
-    // still in L2
-    const int gap = choice_.lag > 0 ? choice_.lag : std::max(1, per_sm_flow_ * num_sms_);
+    // gap: by default three rounds of the grid, so an item is claimed when
+    // the items it waits for have finished (the producer then acquires them
+    // and loads the item's first planes while the block still works on its
+    // previous item) and for grids near the L2 size while their results are
+    // still in L2 (measured at 101^3: one round 31.4, three 32.2 Gcell/s;
+    // neutral from 160^3 up)
+    const int gap = choice_.lag > 0 ? choice_.lag : std::max(1, 3 * per_sm_flow_ * num_sms_);
     if (!build_flow_schedule(shapes, var_->tx, var_->ty, C, gap, choice_.kind == kScheduleFlowOverlap, K, &items,
                              &off, &nch, &nflags, &why))
       BAD(why);

@@ -84,10 +84,10 @@ struct TuneChoice {
   int kind, chunk; // schedule
   int blocks_per_sm;  // 0 = occupancy limit
   int prefetch = kPrefetchDefault;  // CTL_PF_* bits
-  int lag = 0;     // kinds 3, 4: gap in items (0 = one round of the grid)
+  int lag = 0;     // kinds 3, 4: gap in items (0 = three rounds of the grid)
 };
 // Built-in choice when the autotuner's cache has none for the workload.
-TuneChoice default_choice(int fp64, int nx, int ny, int nz);
+TuneChoice default_choice(int fp64, int nx, int ny, int nz, bool explosive = false);
 
 // Autotuner (ela3d_tune.cu): process-wide cache of measured best choices
 // keyed by the workload shape.

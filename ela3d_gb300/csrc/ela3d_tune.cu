@@ -120,7 +120,7 @@ static std::vector<TuneChoice> schedules(int nshots, bool flow) {
     if (nshots > 1)
       for (int ch : {8, 16}) v.push_back({0, 2, ch, 0, pf});
     if (flow) {
-      for (int ch : {4, 6, 8, 16}) v.push_back({0, kScheduleFlowOverlap, ch, 0, pf, 0});
+      for (int ch : {4, 6, 8, 12, 16, 24, 32, 48, 64, 96}) v.push_back({0, kScheduleFlowOverlap, ch, 0, pf, 0});
       for (int ch : {8, 16}) v.push_back({0, kScheduleFlow, ch, 0, pf, 0});
     }
   }

@@ -272,7 +272,7 @@ typedef struct ela3d_tuning {
                                (6, or 2 for a shot that fits in L2) */
     int32_t lag;            /* schedules 3 and 4: places in the work list
                                between an item and the last item it waits
-                               for; 0 or -1 = one round of the grid */
+                               for; 0 or -1 = three rounds of the grid */
 } ela3d_tuning;
 /* Schedules 3 and 4 (dataflow): instead of two kernels per time step, one
  * persistent, cooperative kernel advances up to 50 steps per launch.  Its
@@ -286,7 +286,10 @@ typedef struct ela3d_tuning {
  * explosive source run the two-kernel path with schedule 1.  The work list
  * is built on the host for the shots running, again whenever shots join or
  * retire, so these schedules suit a plan or a batch of shots that run
- * together; the autotuner tries them for single shots. */
+ * together; the autotuner tries them for single shots, and schedule 4 is
+ * the built-in choice for an FP32 shot (without an explosive source) whose
+ * tile columns split into three or more z-chunks at about 1.5 work items
+ * per block (up to about 290^3 cells). */
 
 /* Times every compiled variant with the candidate schedules on these shots
  * (`steps` time steps each, after a warm-up) and returns the fastest choice;
@@ -438,9 +441,11 @@ ela3d_status ela3d_server_destroy(ela3d_server *s);
  * simpelmodel.cpp:89-106).  lo == hi == n when the layer covers the axis. */
 ela3d_status ela3d_slab_extent(const double *a_full, const double *a_half, int32_t n,
                                int32_t *lo, int32_t *hi);
-/* The work split the kernels use for one grid: items (tile, k0, k1) per
- * block.  With items == NULL only the counts are returned.  No reference
- * counterpart (its launch is a fixed 3-D grid, cudazerocopy.cu:1361-1369). */
+/* Host-only: the built-in kernel choice for a single shot with these
+ * parameters (variant, schedule, chunk, prefetch; no tuning cache, no
+ * device work; the current device's SM count, 152 without a device).  No
+ * reference counterpart. */
+ela3d_status ela3d_builtin_tuning(const ela3d_params *p, ela3d_tuning *out);
 /* Host-only test hook: the dataflow work list (schedules 3 and 4) of one
  * nx*ny*nz shot for `nsteps` steps, tiles tile_x*tile_y, z-chunks of
  * `chunk` planes, `gap` places after each item's last dependency, steps
@@ -451,6 +456,9 @@ ela3d_status ela3d_slab_extent(const double *a_full, const double *a_half, int32
 ela3d_status ela3d_flow_schedule_build(int32_t nx, int32_t ny, int32_t nz, int32_t tile_x, int32_t tile_y,
                                        int32_t chunk, int32_t gap, int32_t overlap, int32_t nsteps,
                                        int32_t *nitems, int32_t *items);
+/* The work split the kernels use for one grid: items (tile, k0, k1) per
+ * block.  With items == NULL only the counts are returned.  No reference
+ * counterpart (its launch is a fixed 3-D grid, cudazerocopy.cu:1361-1369). */
 ela3d_status ela3d_schedule_build(int32_t nx, int32_t ny, int32_t nz, int32_t tile_x, int32_t tile_y,
                                   int32_t schedule, int32_t chunk, int32_t max_blocks,
                                   int32_t *nitems, int32_t *nblocks,

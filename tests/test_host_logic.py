@@ -157,3 +157,27 @@ def test_flow_schedule_rejects_bad_arguments(built, chunk, gap):
 
     with pytest.raises(Ela3dError):
         flow_schedule(40, 40, 40, 128, 7, chunk, gap, False, 2)
+
+
+def test_builtin_tuning_by_size():
+    """The built-in choice (ela3d_builtin_tuning, 152 SMs without a device):
+    the dataflow kernel with about 1.5 work items per block while a tile
+    column splits into three or more z-chunks, the two kernels beyond that,
+    for an explosive source and for FP64."""
+    import ela3d_gb300 as E
+    from ela3d_gb300 import configs
+
+    def pick(p):
+        t = E.builtin_tuning(p)
+        v = E.variants()[t.variant]
+        return (v.tile_x, v.tile_y), t.schedule, t.chunk
+
+    assert pick(configs.homogeneous_101()[0]) == ((112, 8), 4, 6)
+    assert pick(configs.anticline_256()[0]) == ((128, 7), 4, 64)
+    assert pick(configs.anticline_256(n=192)[0]) == ((112, 8), 4, 39)
+    assert pick(configs.anticline_256(n=288)[0]) == ((112, 8), 4, 96)
+    assert pick(configs.anticline_256(n=320)[0])[1] == 1
+    assert pick(configs.anticline_256(n=512)[0])[1:] == (1, 32)
+    assert pick(configs.anticline_256()[0].with_(src_kind=E.SRC_EXPLOSIVE))[1:] == (1, 10)
+    t = E.builtin_tuning(configs.anticline_256(precision=E.FP64)[0])
+    assert E.variants()[t.variant].fp64 and t.schedule == 1
