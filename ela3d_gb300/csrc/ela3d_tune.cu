@@ -124,6 +124,12 @@ static std::vector<TuneChoice> schedules(int nshots, bool flow) {
       for (int ch : {8, 16}) v.push_back({0, kScheduleFlow, ch, 0, pf, 0});
     }
   }
+  // the dataflow kernel on grids that fit in L2 runs best without the
+  // memory-variable prefetch
+  if (flow) {
+    for (int ch : {4, 6, 8, 12, 16, 24, 32, 48, 64, 96}) v.push_back({0, kScheduleFlowOverlap, ch, 0, 0, 0});
+    for (int ch : {8, 16}) v.push_back({0, kScheduleFlow, ch, 0, 0, 0});
+  }
   return v;
 }
 

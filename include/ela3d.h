@@ -269,7 +269,8 @@ typedef struct ela3d_tuning {
     int32_t prefetch;       /* prefetch of the C-PML memory variables by the
                                loading warp: bit 1 (2) x slab into L1, bit 2 (4)
                                y and z slabs into L2; -1 = built-in choice
-                               (6, or 2 for a shot that fits in L2) */
+                               (6; 2 or 0 for shots whose arrays fit in or
+                               near the L2) */
     int32_t lag;            /* schedules 3 and 4: places in the work list
                                between an item and the last item it waits
                                for; 0 or -1 = three rounds of the grid */

@@ -179,5 +179,9 @@ def test_builtin_tuning_by_size():
     assert pick(configs.anticline_256(n=320)[0])[1] == 1
     assert pick(configs.anticline_256(n=512)[0])[1:] == (1, 32)
     assert pick(configs.anticline_256()[0].with_(src_kind=E.SRC_EXPLOSIVE))[1:] == (1, 10)
+    # memory-variable prefetch: none while the arrays fit in L2, x slab up
+    # to about twice that, all slabs beyond
+    assert [E.builtin_tuning(p).prefetch for p in (configs.homogeneous_101()[0], configs.anticline_256(n=128)[0],
+                                                   configs.anticline_256()[0])] == [0, 2, 6]
     t = E.builtin_tuning(configs.anticline_256(precision=E.FP64)[0])
     assert E.variants()[t.variant].fp64 and t.schedule == 1
