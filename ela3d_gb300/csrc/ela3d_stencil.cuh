@@ -1117,9 +1117,11 @@ __global__ void __launch_bounds__(Geo<T, TX, TY, NS, CPT, MB>::THREADS, Geo<T, T
 // ------------------------------------------------- dataflow kernel ----
 // Many time steps in one persistent launch.  The work is a list of items,
 // each the stress or the velocity half-step of one (shot, x-y tile,
-// z-chunk) at one step of the launch (items of steps >= nsteps are
+// z-chunk) at one of list_steps steps; a launch of nsteps steps walks the
+// list again for every further list_steps steps (the item of list step s
+// in pass p runs step p * list_steps + s; items of steps >= nsteps are
 // skipped, so one list serves shorter launches); block b takes items
-// b, b + G, ...
+// b, b + G, ... of every pass
 // (G blocks, all resident: the launch is cooperative).  Chunk j of a shot
 // covers planes [jC, (j+1)C) for stress and the same range shifted down by
 // one plane for velocity, so that
@@ -1228,8 +1230,8 @@ __device__ __forceinline__ bool flow_wait_deps(const ShotDesc<T> &sd, const Flow
 template <typename T, int TX, int TY, int NS, int CPT, int MB>
 __global__ void __launch_bounds__(Geo<T, TX, TY, NS, CPT, MB>::THREADS, Geo<T, TX, TY, NS, CPT, MB>::MINB)
     flow_kernel(const ShotDesc<T> *__restrict__ shots, const ShotMaps *__restrict__ maps,
-                const FlowItem *__restrict__ items, int nitems, int nsteps, int tick, const int *__restrict__ dtick,
-                unsigned *__restrict__ err, int ctl) {
+                const FlowItem *__restrict__ items, int nitems, int list_steps, int nsteps, int tick,
+                const int *__restrict__ dtick, unsigned *__restrict__ err, int ctl) {
   using G = Geo<T, TX, TY, NS, CPT, MB>;
   using F = Flow<T, TX, TY, NS, CPT, MB>;
   extern __shared__ __align__(1024) unsigned char smem[];
@@ -1253,8 +1255,10 @@ __global__ void __launch_bounds__(Geo<T, TX, TY, NS, CPT, MB>::THREADS, Geo<T, T
     ItemPrefetch<T, TX, TY> pf_v{{}, shots, lane, ctl, PSI_V0};
     unsigned n = 0, idx = 0;
     bool ok = true;
+    for (int rep = 0; rep < nsteps && ok; rep += list_steps)
     for (int q = blockIdx.x; q < nitems && ok; q += gridDim.x) {
-      const FlowItem fi = items[q];
+      FlowItem fi = items[q];
+      fi.step += rep;
       if (fi.step >= nsteps) continue;   // a list of more steps than this launch runs
       const ShotDesc<T> &sd = shots[fi.it.shot];
       int good = 1;
@@ -1287,8 +1291,10 @@ __global__ void __launch_bounds__(Geo<T, TX, TY, NS, CPT, MB>::THREADS, Geo<T, T
   const int lane = tid & 31, warp = tid >> 5;
   if (dtick) tick += *dtick;
   unsigned n = 0, idx = 0;
+  for (int rep = 0; rep < nsteps; rep += list_steps)
   for (int q = blockIdx.x; q < nitems; q += gridDim.x) {
-    const FlowItem fi = items[q];
+    FlowItem fi = items[q];
+    fi.step += rep;
     if (fi.step >= nsteps) continue;
     const ShotDesc<T> &sd = shots[fi.it.shot];
     uint64_t *rb = &ready[idx % F::RB];

@@ -129,14 +129,22 @@ def test_flow_explosive_source_runs_two_kernels(built):
 
 
 def test_flow_timing_and_launch_count(built):
+    """A launch walks its 50-step list up to four times: 450 steps take
+    launches of 200, 200 and 50 steps, with the results of 50-step ones."""
     from ela3d_gb300 import Plan
 
-    p, cp, cs, rho = _shot(nstep=120)
+    p, cp, cs, rho = _shot(nstep=450)
     with Plan(p, cp, cs, rho, variant=0, schedule=4, chunk=8) as plan:
         plan.set_kernel_timing(True)
-        plan.run(120)
+        plan.run(450)
         ms, launches, steps = plan.flow_timing()
-    assert launches == 3 and steps == 120 and ms > 0
+        got = (plan.seismograms(), plan.field(2))
+    assert launches == 3 and steps == 450 and ms > 0
+    with Plan(p, cp, cs, rho, variant=0, schedule=4, chunk=8) as plan:
+        for _ in range(9):
+            plan.run(50)
+        want = (plan.seismograms(), plan.field(2))
+    assert all(np.array_equal(a, b) for a, b in zip(got, want))
 
 
 def test_flow_timeout_path(built):
