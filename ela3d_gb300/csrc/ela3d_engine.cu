@@ -189,8 +189,8 @@ bool build_flow_schedule(const std::vector<FlowShape> &shots, int tx, int ty, in
   flag_off->clear();
   nchunks->clear();
   *nflags = 0;
-  if (chunk < 2 || gap < 1 || nsteps < 1 || tx < 1 || ty < 1) {
-    *why = "dataflow schedule: chunk >= 2, gap >= 1, nsteps >= 1";
+  if (chunk < 2 || gap < 1 || nsteps < 1 || nsteps > 255 || tx < 1 || ty < 1 || shots.size() >= (1u << 16)) {
+    *why = "dataflow schedule: chunk >= 2, gap >= 1, 1 <= nsteps <= 255, fewer than 65536 shots";
     return false;
   }
   // Keys approximate list positions (two per stress item of one step in
@@ -206,6 +206,11 @@ bool build_flow_schedule(const std::vector<FlowShape> &shots, int tx, int ty, in
     const FlowShape &sh = shots[s];
     const int txs = (sh.nx + tx - 1) / tx, tys = (sh.ny + ty - 1) / ty, nt = txs * tys;
     const int J = (sh.nz + chunk - 1) / chunk;
+    if (J >= (1 << 14) || nt >= (1 << 25)) {
+      *why = "dataflow schedule: too many z-chunks or tiles for one shot";
+      return false;
+    }
+    all.reserve(all.size() + (size_t)nsteps * 2 * J * nt);
     txs_of.push_back(txs);
     tys_of.push_back(tys);
     flag_off->push_back(*nflags);
@@ -248,14 +253,26 @@ bool build_flow_schedule(const std::vector<FlowShape> &shots, int tx, int ty, in
       if (!overlap) step_base = *std::max_element(kv.begin(), kv.end()) + 1;
     }
   }
-  std::stable_sort(all.begin(), all.end(), [](const Keyed &a, const Keyed &b) {
-    if (a.key != b.key) return a.key < b.key;
-    if (a.step != b.step) return a.step < b.step;
-    if (a.kind != b.kind) return a.kind < b.kind;
-    if (a.shot != b.shot) return a.shot < b.shot;
-    if (a.chunk != b.chunk) return a.chunk < b.chunk;
-    return a.tile < b.tile;
+  // order by key, ties by (step, kind, shot, chunk, tile): sorted as
+  // (key, packed tie, index) records, a third of the bytes of the items
+  struct Ord { long long key; unsigned long long tie; unsigned idx; };
+  std::vector<Ord> ord(all.size());
+  for (size_t q = 0; q < all.size(); ++q) {
+    const Keyed &a = all[q];
+    const unsigned long long tie = ((unsigned long long)a.step << 56) | ((unsigned long long)a.kind << 55) |
+                                   ((unsigned long long)a.shot << 39) | ((unsigned long long)a.chunk << 25) |
+                                   (unsigned long long)a.tile;
+    ord[q] = {a.key, tie, (unsigned)q};
+  }
+  std::sort(ord.begin(), ord.end(), [](const Ord &a, const Ord &b) {
+    return a.key != b.key ? a.key < b.key : a.tie < b.tie;
   });
+  {
+    std::vector<Keyed> sorted;
+    sorted.reserve(all.size());
+    for (const Ord &o : ord) sorted.push_back(all[o.idx]);
+    all.swap(sorted);
+  }
   // check: every item comes after every item it waits for
   std::vector<std::vector<int>> pos(shots.size());
   for (size_t s = 0; s < shots.size(); ++s)
