@@ -198,104 +198,120 @@ bool build_flow_schedule(const std::vector<FlowShape> &shots, int tx, int ty, in
   // stress item of step 0 sits at its natural place, every other item `gap`
   // after the last item it waits for (a stress item of a later step also
   // no earlier than its natural place, plus the whole steps before it
-  // unless steps may overlap).
-  struct Keyed { long long key; int shot, step, kind, chunk, tile; FlowItem fi; };
-  std::vector<Keyed> all;
-  std::vector<int> txs_of, tys_of;
-  for (int s = 0; s < (int)shots.size(); ++s) {
-    const FlowShape &sh = shots[s];
-    const int txs = (sh.nx + tx - 1) / tx, tys = (sh.ny + ty - 1) / ty, nt = txs * tys;
-    const int J = (sh.nz + chunk - 1) / chunk;
-    if (J >= (1 << 14) || nt >= (1 << 25)) {
+  // unless steps may overlap).  The list is ordered by key, ties by (step,
+  // kind, shot, chunk, tile): the items are generated in that tie order and
+  // sorted stably by key (a counting sort when the keys are dense).
+  struct Shape { int txs, tys, nt, J; long long step_base; std::vector<long long> ks, kv, kv_prev; };
+  std::vector<Shape> sh(shots.size());
+  size_t total = 0;
+  for (size_t s = 0; s < shots.size(); ++s) {
+    Shape &h = sh[s];
+    h.txs = (shots[s].nx + tx - 1) / tx;
+    h.tys = (shots[s].ny + ty - 1) / ty;
+    h.nt = h.txs * h.tys;
+    h.J = (shots[s].nz + chunk - 1) / chunk;
+    if (h.J >= (1 << 14) || h.nt >= (1 << 25)) {
       *why = "dataflow schedule: too many z-chunks or tiles for one shot";
       return false;
     }
-    all.reserve(all.size() + (size_t)nsteps * 2 * J * nt);
-    txs_of.push_back(txs);
-    tys_of.push_back(tys);
+    h.step_base = 0;
+    h.ks.assign((size_t)h.J * h.nt, 0);
+    h.kv.assign((size_t)h.J * h.nt, 0);
     flag_off->push_back(*nflags);
-    nchunks->push_back(J);
-    *nflags += 2 * J * nt;
-    std::vector<long long> ks((size_t)J * nt), kv((size_t)J * nt), ks_prev, kv_prev;
-    auto idx = [&](int j, int t) { return (size_t)j * nt + t; };
-    // the items one item waits for (chunks c0/c1 of the other kind, on the
-    // tile and its four neighbours): the largest key among them
-    auto last_dep = [&](const std::vector<long long> &k, int c0, int c1, int t) {
-      const int x = t % txs, y = t / txs;
-      const int nb[5][2] = {{x, y}, {x - 1, y}, {x + 1, y}, {x, y - 1}, {x, y + 1}};
-      long long m = -1;
-      for (auto &b : nb) {
-        if (b[0] < 0 || b[0] >= txs || b[1] < 0 || b[1] >= tys) continue;
-        for (int c : {c0, c1})
-          if (c >= 0 && c < J) m = std::max(m, k[idx(c, b[1] * txs + b[0])]);
-      }
-      return m;
-    };
-    long long step_base = 0;   // without overlap: past every key of the previous step
-    for (int r = 0; r < nsteps; ++r) {
-      for (int j = 0; j < J; ++j)
-        for (int t = 0; t < nt; ++t) {
-          long long key = 2ll * ((long long)j * nt + t) + step_base;
-          if (r > 0) key = std::max(key, last_dep(kv_prev, j, j + 1, t) + gap);
-          ks[idx(j, t)] = key;
-          const int k0 = j * chunk, k1 = std::min((j + 1) * chunk, sh.nz);
-          all.push_back({key, s, r, 0, j, t, FlowItem{{sh.id, t, k0, k1}, 0, r, j, 0}});
+    nchunks->push_back(h.J);
+    *nflags += 2 * h.J * h.nt;
+    total += (size_t)nsteps * 2 * h.J * h.nt;
+  }
+  // the items one item waits for (chunks c0/c1 of the other kind, on the
+  // tile and its four neighbours): the largest key among them
+  auto last_dep = [](const Shape &h, const std::vector<long long> &k, int c0, int c1, int t) {
+    const int x = t % h.txs, y = t / h.txs;
+    const int nb[5][2] = {{x, y}, {x - 1, y}, {x + 1, y}, {x, y - 1}, {x, y + 1}};
+    long long m = -1;
+    for (auto &b : nb) {
+      if (b[0] < 0 || b[0] >= h.txs || b[1] < 0 || b[1] >= h.tys) continue;
+      for (int c : {c0, c1})
+        if (c >= 0 && c < h.J) m = std::max(m, k[(size_t)c * h.nt + b[1] * h.txs + b[0]]);
+    }
+    return m;
+  };
+  std::vector<FlowItem> gen;
+  std::vector<long long> key;
+  std::vector<int> shot_of;
+  gen.reserve(total);
+  key.reserve(total);
+  shot_of.reserve(total);
+  for (int r = 0; r < nsteps; ++r) {
+    for (size_t s = 0; s < shots.size(); ++s) {   // stress items of step r
+      Shape &h = sh[s];
+      for (int j = 0; j < h.J; ++j)
+        for (int t = 0; t < h.nt; ++t) {
+          long long k = 2ll * ((long long)j * h.nt + t) + h.step_base;
+          if (r > 0) k = std::max(k, last_dep(h, h.kv_prev, j, j + 1, t) + gap);
+          h.ks[(size_t)j * h.nt + t] = k;
+          const int k0 = j * chunk, k1 = std::min((j + 1) * chunk, shots[s].nz);
+          gen.push_back(FlowItem{{shots[s].id, t, k0, k1}, 0, r, j, 0});
+          key.push_back(k);
+          shot_of.push_back((int)s);
         }
-      for (int j = 0; j < J; ++j)
-        for (int t = 0; t < nt; ++t) {
-          const long long key = last_dep(ks, j - 1, j, t) + gap;
-          kv[idx(j, t)] = key;
-          const int k0 = std::max(j * chunk - 1, 0), k1 = (j == J - 1) ? sh.nz : (j + 1) * chunk - 1;
-          all.push_back({key, s, r, 1, j, t, FlowItem{{sh.id, t, k0, k1}, 1, r, j, 0}});
+    }
+    for (size_t s = 0; s < shots.size(); ++s) {   // velocity items of step r
+      Shape &h = sh[s];
+      for (int j = 0; j < h.J; ++j)
+        for (int t = 0; t < h.nt; ++t) {
+          const long long k = last_dep(h, h.ks, j - 1, j, t) + gap;
+          h.kv[(size_t)j * h.nt + t] = k;
+          const int k0 = std::max(j * chunk - 1, 0), k1 = (j == h.J - 1) ? shots[s].nz : (j + 1) * chunk - 1;
+          gen.push_back(FlowItem{{shots[s].id, t, k0, k1}, 1, r, j, 0});
+          key.push_back(k);
+          shot_of.push_back((int)s);
         }
-      ks_prev = ks;
-      kv_prev = kv;
-      if (!overlap) step_base = *std::max_element(kv.begin(), kv.end()) + 1;
+      h.kv_prev = h.kv;
+      if (!overlap) h.step_base = *std::max_element(h.kv.begin(), h.kv.end()) + 1;
     }
   }
-  // order by key, ties by (step, kind, shot, chunk, tile): sorted as
-  // (key, packed tie, index) records, a third of the bytes of the items
-  struct Ord { long long key; unsigned long long tie; unsigned idx; };
-  std::vector<Ord> ord(all.size());
-  for (size_t q = 0; q < all.size(); ++q) {
-    const Keyed &a = all[q];
-    const unsigned long long tie = ((unsigned long long)a.step << 56) | ((unsigned long long)a.kind << 55) |
-                                   ((unsigned long long)a.shot << 39) | ((unsigned long long)a.chunk << 25) |
-                                   (unsigned long long)a.tile;
-    ord[q] = {a.key, tie, (unsigned)q};
+  // stable sort by key
+  const size_t n = gen.size();
+  std::vector<unsigned> order(n);
+  long long kmin = 0, kmax = -1;
+  if (n) {
+    kmin = *std::min_element(key.begin(), key.end());
+    kmax = *std::max_element(key.begin(), key.end());
   }
-  std::sort(ord.begin(), ord.end(), [](const Ord &a, const Ord &b) {
-    return a.key != b.key ? a.key < b.key : a.tie < b.tie;
-  });
-  {
-    std::vector<Keyed> sorted;
-    sorted.reserve(all.size());
-    for (const Ord &o : ord) sorted.push_back(all[o.idx]);
-    all.swap(sorted);
+  const unsigned long long range = n ? (unsigned long long)(kmax - kmin) + 1 : 0;
+  if (n && range <= 16ull * n + 1024) {
+    std::vector<unsigned> cnt(range + 1, 0);
+    for (size_t q = 0; q < n; ++q) ++cnt[key[q] - kmin + 1];
+    for (size_t v = 1; v <= range; ++v) cnt[v] += cnt[v - 1];
+    for (size_t q = 0; q < n; ++q) order[cnt[key[q] - kmin]++] = (unsigned)q;
+  } else {
+    for (size_t q = 0; q < n; ++q) order[q] = (unsigned)q;
+    std::stable_sort(order.begin(), order.end(), [&](unsigned a, unsigned b) { return key[a] < key[b]; });
   }
   // check: every item comes after every item it waits for
   std::vector<std::vector<int>> pos(shots.size());
-  for (size_t s = 0; s < shots.size(); ++s)
-    pos[s].assign((size_t)nsteps * 2 * (*nchunks)[s] * txs_of[s] * tys_of[s], -1);
+  for (size_t s = 0; s < shots.size(); ++s) pos[s].assign((size_t)nsteps * 2 * sh[s].J * sh[s].nt, -1);
   auto at = [&](int s, int r, int kind, int j, int t) -> int & {
-    const int J = (*nchunks)[s], nt = txs_of[s] * tys_of[s];
-    return pos[s][(((size_t)r * 2 + kind) * J + j) * nt + t];
+    return pos[s][(((size_t)r * 2 + kind) * sh[s].J + j) * sh[s].nt + t];
   };
-  for (size_t q = 0; q < all.size(); ++q) at(all[q].shot, all[q].step, all[q].kind, all[q].chunk, all[q].tile) = (int)q;
-  for (size_t q = 0; q < all.size(); ++q) {
-    const int s = all[q].shot;
-    const FlowItem &f = all[q].fi;
-    const int txs = txs_of[s], tys = tys_of[s], J = (*nchunks)[s];
-    const int tx0 = f.it.tile % txs, ty0 = f.it.tile / txs;
+  for (size_t q = 0; q < n; ++q) {
+    const FlowItem &f = gen[order[q]];
+    at(shot_of[order[q]], f.step, f.kind, f.chunk, f.it.tile) = (int)q;
+  }
+  for (size_t q = 0; q < n; ++q) {
+    const int s = shot_of[order[q]];
+    const FlowItem &f = gen[order[q]];
+    const Shape &h = sh[s];
+    const int tx0 = f.it.tile % h.txs, ty0 = f.it.tile / h.txs;
     const int r = f.kind == 0 ? f.step - 1 : f.step;   // step of the items waited for
     if (r < 0) continue;                               // before the launch: done
-    const int c0 = f.chunk, c1 = f.kind == 0 ? (f.chunk + 1 < J ? f.chunk + 1 : -1) : f.chunk - 1;
+    const int c0 = f.chunk, c1 = f.kind == 0 ? (f.chunk + 1 < h.J ? f.chunk + 1 : -1) : f.chunk - 1;
     const int nb[5][2] = {{tx0, ty0}, {tx0 - 1, ty0}, {tx0 + 1, ty0}, {tx0, ty0 - 1}, {tx0, ty0 + 1}};
     for (auto &b : nb) {
-      if (b[0] < 0 || b[0] >= txs || b[1] < 0 || b[1] >= tys) continue;
+      if (b[0] < 0 || b[0] >= h.txs || b[1] < 0 || b[1] >= h.tys) continue;
       for (int c : {c0, c1}) {
         if (c < 0) continue;
-        const int d = at(s, r, 1 - f.kind, c, b[1] * txs + b[0]);
+        const int d = at(s, r, 1 - f.kind, c, b[1] * h.txs + b[0]);
         if (d < 0 || d >= (int)q) {
           *why = "dataflow schedule: an item does not follow the items it waits for";
           return false;
@@ -303,8 +319,8 @@ bool build_flow_schedule(const std::vector<FlowShape> &shots, int tx, int ty, in
       }
     }
   }
-  items->reserve(all.size());
-  for (auto &k : all) items->push_back(k.fi);
+  items->resize(n);
+  for (size_t q = 0; q < n; ++q) (*items)[q] = gen[order[q]];
   return true;
 }
 
