@@ -276,7 +276,7 @@ typedef struct ela3d_tuning {
                                for; 0 or -1 = three rounds of the grid */
 } ela3d_tuning;
 /* Schedules 3 and 4 (dataflow): instead of two kernels per time step, one
- * persistent, cooperative kernel advances up to 50 steps per launch.  Its
+ * persistent, cooperative kernel advances up to 200 steps per launch.  Its
  * work items are the stress or velocity half-step of one (x-y tile,
  * z-chunk) at one step; each item waits (on device counters) for exactly
  * the items whose results it reads or overwrites.  The host places every
