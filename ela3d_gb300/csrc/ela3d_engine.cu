@@ -368,20 +368,22 @@ TuneChoice default_choice(int fp64, int nx, int ny, int nz, bool explosive) {
     // y/z-slab memory variables into L2 ahead of use
     const double bytes = 12.0 * nx * ny * nz * (fp64 ? 8.0 : 4.0);
     if (bytes < 96.0 * (1 << 20)) c.prefetch = CTL_PF_X;
-    // FP32 shots run faster in the dataflow kernel with overlapping steps
-    // when the half-step's work items (tile columns cut into z-chunks) number
-    // about 1.5 per block with at least three chunks per column: no launch
-    // boundaries, no tail of a half-step, and for grids near the L2 size the
-    // exchange between the half-steps through L2.  Measured (Gcell/s,
-    // dataflow against the best two-kernel chunk): 101^3 32.2 vs 26.4,
-    // 128^3 29.7 vs 22.5, 160^3 30.8 vs 25.9, 192^3 38.9 vs 34.1, 224^3
-    // 42.6 vs 40.8, 256^3 45.6 vs 44.5, 288^3 42.0 vs 41.2; at 320^3 (two
-    // chunks per column) the two kernels stay ahead, 43.5 vs 42.5.  An
-    // explosive source injects between the half-steps, so it keeps the
-    // two kernels.
+    // FP32 shots run faster in the dataflow kernel with overlapping steps:
+    // no launch boundaries, no tail of a half-step, and for grids near the
+    // L2 size the exchange between the half-steps through L2.  Its work
+    // items (tile columns cut into z-chunks) number about 1.5 per block,
+    // with at least three chunks per column while the columns alone are
+    // fewer than that, whole columns beyond.  Measured (Gcell/s, dataflow
+    // against the best two-kernel choice): 101^3 32.2 vs 26.4, 128^3 29.7
+    // vs 22.5, 160^3 30.8 vs 25.9, 192^3 38.9 vs 34.1, 224^3 42.6 vs 40.8,
+    // 256^3 45.6 vs 44.5, 288^3 42.0 vs 41.2, 384^3 46.1 vs 44.9, 448^3
+    // 42.2 vs 41.8, 512^3 47.0 vs 45.4, 1024^3 47.6 vs 44.7; only 320^3 is
+    // the other way, 42.8 vs 43.4.  An explosive source injects between the
+    // half-steps, so it keeps the two kernels.
     if (!fp64 && !explosive && v[i].flow) {
-      const long long per_col = (3ll * sms / 2 + tiles - 1) / tiles;   // z-chunks per tile column
-      if (per_col >= 3) {
+      const long long want = 3ll * sms / 2;                              // work items per half-step
+      const long long per_col = want <= tiles ? 1 : std::max(3ll, (want + tiles - 1) / tiles);
+      {
         c.kind = kScheduleFlowOverlap;
         c.chunk = std::max(4, (int)((nz + per_col - 1) / per_col));
         c.lag = 0;

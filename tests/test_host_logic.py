@@ -161,9 +161,9 @@ def test_flow_schedule_rejects_bad_arguments(built, chunk, gap):
 
 def test_builtin_tuning_by_size():
     """The built-in choice (ela3d_builtin_tuning, 152 SMs without a device):
-    the dataflow kernel with about 1.5 work items per block while a tile
-    column splits into three or more z-chunks, the two kernels beyond that,
-    for an explosive source and for FP64."""
+    the dataflow kernel with about 1.5 work items per block (three or more
+    z-chunks per tile column while the columns are fewer, whole columns
+    beyond); the two kernels for an explosive source and for FP64."""
     import ela3d_gb300 as E
     from ela3d_gb300 import configs
 
@@ -176,8 +176,8 @@ def test_builtin_tuning_by_size():
     assert pick(configs.anticline_256()[0]) == ((128, 7), 4, 64)
     assert pick(configs.anticline_256(n=192)[0]) == ((112, 8), 4, 39)
     assert pick(configs.anticline_256(n=288)[0]) == ((112, 8), 4, 96)
-    assert pick(configs.anticline_256(n=320)[0])[1] == 1
-    assert pick(configs.anticline_256(n=512)[0])[1:] == (1, 32)
+    assert pick(configs.anticline_256(n=320)[0]) == ((112, 8), 4, 107)   # three chunks per column at least
+    assert pick(configs.anticline_256(n=512)[0])[1:] == (4, 512)          # whole columns: 296 tiles
     assert pick(configs.anticline_256()[0].with_(src_kind=E.SRC_EXPLOSIVE))[1:] == (1, 10)
     # memory-variable prefetch: none while the arrays fit in L2, x slab up
     # to about twice that, all slabs beyond
