@@ -372,8 +372,10 @@ def run_ours(args, rank, world, local):
     t_max = dist.max(ms / 1e3)
     value = cells * args.steps * world / t_max / 1e9
     if f_launches:
-        # dataflow kernel: one launch per (up to) 50 steps
-        launches = -(-args.steps // 50)
+        # dataflow kernel: one launch per up to 200 steps (its 50-step work
+        # list walked up to four times; the kernel-timing pass reports the
+        # same split: f_launches launches for f_steps steps)
+        launches = -(-args.steps // 200)
     else:
         # kernels launched in the timed region: one step-counter set, 50-step
         # graphs of 100 stencil launches plus a counter update, the rest direct
