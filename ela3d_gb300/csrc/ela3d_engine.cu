@@ -1123,9 +1123,10 @@ class Engine final : public EngineBase {
     return ELA3D_OK;
   }
 
-  // The dataflow list of the active shots for up to kFlowSteps steps per
-  // launch (fewer when the list would pass kFlowMaxItems items), their
-  // completion counters, and the descriptors that point at them.
+  // The dataflow list of the active shots for up to kFlowSteps steps (fewer
+  // when the list would pass kFlowMaxItems items; a launch walks it up to
+  // flow_passes_ times), their completion counters, and the descriptors that
+  // point at them.
   ela3d_status rebuild_flow(const std::vector<int> &active) {
     std::vector<FlowShape> shapes;
     long long per_step = 0;

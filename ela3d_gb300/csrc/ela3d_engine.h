@@ -56,9 +56,11 @@ void build_schedule(const std::vector<ShotShape> &shots, int tx, int ty, int kin
 // neighbours; velocity waits for stress of chunks j-1, j at step r there.
 // Order: a stress item of step 0 at its natural place (chunk by chunk,
 // tile by tile), every other item `gap` places after the last item it
-// waits for -- about one round of the grid, so that it is claimed when
-// those have finished while their results are still in L2; stress items of
-// a later step come after the whole previous step unless `overlap`.  Every
+// waits for -- by default three rounds of the grid, so that it is claimed
+// when those have finished (for grids near the L2 size, while their results
+// are still in L2); stress items of a later step come after the whole
+// previous step unless `overlap`.  The list is generated in tie order and
+// sorted stably by key; 1 <= nsteps <= 255.  Every
 // item is checked to follow the items it waits for, which is what makes
 // the kernel's waits end.  flag_off[s] is shot s's offset into the
 // completion counters ([2][chunks][tiles] ints each), *nflags their total.
@@ -75,8 +77,8 @@ bool build_flow_schedule(const std::vector<FlowShape> &shots, int tx, int ty, in
 constexpr int kPrefetchDefault = CTL_PF_X | CTL_PF_YZ;
 // Schedule kinds 0-2 launch the two half-step kernels once per step; kinds
 // 3 and 4 run many steps per launch of the dataflow kernel (chunk planes
-// per z-chunk, lag = the gap of build_flow_schedule, 0 = one round of the
-// grid; kind 4 lets consecutive steps overlap).
+// per z-chunk, lag = the gap of build_flow_schedule, 0 = three rounds of
+// the grid; kind 4 lets consecutive steps overlap).
 constexpr int kScheduleFlow = 3;
 constexpr int kScheduleFlowOverlap = 4;
 struct TuneChoice {
