@@ -510,7 +510,7 @@ class Engine final : public EngineBase {
     CK(cudaMalloc(&d_tick_, sizeof(int)));
     CK(cudaMemset(d_tick_, 0, sizeof(int)));
     if (const char *e = std::getenv("ELA3D_GRAPH_STEPS")) graph_steps_ = std::max(1, std::atoi(e));
-    if (const char *e = std::getenv("ELA3D_FLOW_STEPS")) flow_max_steps_ = std::max(1, std::atoi(e));
+    if (const char *e = std::getenv("ELA3D_FLOW_STEPS")) flow_max_steps_ = std::min(255, std::max(1, std::atoi(e)));
     if (const char *e = std::getenv("ELA3D_FLOW_PASSES")) flow_passes_ = std::max(1, std::atoi(e));
     // ELA3D_PSI_PREFETCH=<bits> overrides the tuned prefetch mode (experiments)
     if (const char *e = std::getenv("ELA3D_PSI_PREFETCH")) prefetch_env_ = std::atoi(e) & (CTL_PF_X | CTL_PF_YZ);
