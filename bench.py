@@ -449,7 +449,7 @@ def run_ours(args, rank, world, local):
         extra["large_grid"] = large_grid(args.large)
     if not args.no_batched:
         extra["batched"] = batched_shots(args, value, e2e["value"] if e2e else None)   # shots split across ranks
-        if world == 1:
+        if world == 1 and not args.batched_only:
             extra["uneven"] = uneven_batch(args)
             extra["serving"] = serving(args)
 
@@ -1060,6 +1060,8 @@ def main():
                     help="skip the FP64 re-run of the end-to-end shot (accuracy of every seismogram and field)")
     ap.add_argument("--no-batched", action="store_true",
                     help="skip the batched, uneven, serving and larger-grid workloads")
+    ap.add_argument("--batched-only", action="store_true",
+                    help="of the batched, uneven and serving workloads run only the first (profiling runs)")
     ap.add_argument("--no-autotune", action="store_true", help="use the built-in kernel choice")
     ap.add_argument("--prefetch", type=int, default=-1,
                     help="C-PML memory-variable prefetch mode of the single-shot plan (ela3d_tuning.prefetch: "
