@@ -161,7 +161,17 @@ ela3d_status autotune(const std::vector<ela3d_params> &ps, const std::vector<con
     if (st != ELA3D_OK) continue;
     // the dataflow list is rebuilt on the host whenever shots join or
     // retire, which batches and servers do: it is tried for single shots
-    for (TuneChoice c : schedules((int)ps.size(), vs[v].flow != nullptr && ps.size() == 1)) {
+    std::vector<TuneChoice> cands = schedules((int)ps.size(), vs[v].flow != nullptr && ps.size() == 1);
+    if (ps.size() == 1) {
+      // the built-in choice for this shot is always among the candidates
+      // (its chunk is sized to the shot)
+      const TuneChoice d = default_choice(fp64, ps[0].nx, ps[0].ny, ps[0].nz, ps[0].src_kind == ELA3D_SRC_EXPLOSIVE);
+      bool have = d.variant != v;
+      for (const TuneChoice &c : cands)
+        have = have || (c.kind == d.kind && c.chunk == d.chunk && c.prefetch == d.prefetch && c.lag == d.lag);
+      if (!have) cands.push_back({0, d.kind, d.chunk, 0, d.prefetch, d.lag});
+    }
+    for (TuneChoice c : cands) {
       c.variant = v;
       st = eng->retune(c);
       if (st == ELA3D_OK) st = eng->enqueue(2);  // warm-up

@@ -173,7 +173,7 @@ def test_builtin_tuning_by_size():
         return (v.tile_x, v.tile_y), t.schedule, t.chunk
 
     assert pick(configs.homogeneous_101()[0]) == ((112, 8), 4, 6)
-    assert pick(configs.anticline_256()[0]) == ((128, 7), 4, 64)
+    assert pick(configs.anticline_256()[0]) == ((128, 7), 4, 86)
     assert pick(configs.anticline_256(n=192)[0]) == ((112, 8), 4, 39)
     assert pick(configs.anticline_256(n=288)[0]) == ((112, 8), 4, 96)
     assert pick(configs.anticline_256(n=320)[0]) == ((112, 8), 4, 107)   # three chunks per column at least
