@@ -109,7 +109,10 @@ def _flow_deps(item, J, txs, tys):
                                                           ((101, 101, 101), (128, 7), 8, 152, True),
                                                           ((70, 45, 33), (64, 14), 5, 3, True),
                                                           ((40, 30, 9), (128, 3), 2, 1, False),
-                                                          ((40, 30, 9), (128, 3), 16, 40, True)])
+                                                          ((40, 30, 9), (128, 3), 16, 40, True),
+                                                          # keys too sparse for the counting sort: the
+                                                          # comparison-sort path
+                                                          ((40, 30, 9), (128, 3), 2, 100000, False)])
 def test_flow_schedule_covers_every_update_once_in_dependency_order(built, shape, tile, chunk, gap, overlap):
     from ela3d_gb300._abi import flow_schedule
 
@@ -150,13 +153,13 @@ def test_flow_schedule_covers_every_update_once_in_dependency_order(built, shape
         assert overlapped
 
 
-@pytest.mark.parametrize("chunk,gap", [(1, 10), (4, 0), (0, 5)])
-def test_flow_schedule_rejects_bad_arguments(built, chunk, gap):
+@pytest.mark.parametrize("chunk,gap,steps", [(1, 10, 2), (4, 0, 2), (0, 5, 2), (4, 10, 0), (4, 10, 256)])
+def test_flow_schedule_rejects_bad_arguments(built, chunk, gap, steps):
     from ela3d_gb300 import Ela3dError
     from ela3d_gb300._abi import flow_schedule
 
     with pytest.raises(Ela3dError):
-        flow_schedule(40, 40, 40, 128, 7, chunk, gap, False, 2)
+        flow_schedule(40, 40, 40, 128, 7, chunk, gap, False, steps)
 
 
 def test_builtin_tuning_by_size():
