@@ -288,9 +288,9 @@ typedef struct ela3d_tuning {
  * is built on the host for the shots running, again whenever shots join or
  * retire, so these schedules suit a plan or a batch of shots that run
  * together; the autotuner tries them for single shots, and schedule 4 is
- * the built-in choice for an FP32 shot (without an explosive source) whose
- * tile columns split into three or more z-chunks at about 1.5 work items
- * per block (up to about 290^3 cells). */
+ * the built-in choice for a single FP32 shot without an explosive source,
+ * its z-chunks sized for about 1.5 work items per block (ela3d_builtin_tuning
+ * reports the choice). */
 
 /* Times every compiled variant with the candidate schedules on these shots
  * (`steps` time steps each, after a warm-up) and returns the fastest choice;
