@@ -1247,6 +1247,7 @@ __global__ void __launch_bounds__(Geo<T, TX, TY, NS, CPT, MB>::THREADS, Geo<T, T
     }
   init_ring<NS, G::NCW, LOAD_TMA>(full, empty);
   const unsigned long long wait_ns = (ctl & CTL_WITHHOLD_LOADS) ? kTestWaitLimitNs : kWaitLimitNs;
+  const int pass_steps = list_steps > 0 ? list_steps : nsteps;   // (one pass if the list's length is unset)
 
   if (tid >= G::NT) {  // producer warp
     const int lane = tid - G::NT;
@@ -1255,7 +1256,7 @@ __global__ void __launch_bounds__(Geo<T, TX, TY, NS, CPT, MB>::THREADS, Geo<T, T
     ItemPrefetch<T, TX, TY> pf_v{{}, shots, lane, ctl, PSI_V0};
     unsigned n = 0, idx = 0;
     bool ok = true;
-    for (int rep = 0; rep < nsteps && ok; rep += list_steps)
+    for (int rep = 0; rep < nsteps && ok; rep += pass_steps)
     for (int q = blockIdx.x; q < nitems && ok; q += gridDim.x) {
       FlowItem fi = items[q];
       // the block's next work item into L1: its consumers read it at their
@@ -1297,7 +1298,7 @@ __global__ void __launch_bounds__(Geo<T, TX, TY, NS, CPT, MB>::THREADS, Geo<T, T
   const int lane = tid & 31, warp = tid >> 5;
   if (dtick) tick += *dtick;
   unsigned n = 0, idx = 0;
-  for (int rep = 0; rep < nsteps; rep += list_steps)
+  for (int rep = 0; rep < nsteps; rep += pass_steps)
   for (int q = blockIdx.x; q < nitems; q += gridDim.x) {
     FlowItem fi = items[q];
     fi.step += rep;
