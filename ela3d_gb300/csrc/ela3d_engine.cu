@@ -224,48 +224,51 @@ bool build_flow_schedule(const std::vector<FlowShape> &shots, int tx, int ty, in
   }
   // the items one item waits for (chunks c0/c1 of the other kind, on the
   // tile and its four neighbours): the largest key among them
-  auto last_dep = [](const Shape &h, const std::vector<long long> &k, int c0, int c1, int t) {
-    const int x = t % h.txs, y = t / h.txs;
-    const int nb[5][2] = {{x, y}, {x - 1, y}, {x + 1, y}, {x, y - 1}, {x, y + 1}};
+  auto last_dep = [](const Shape &h, const std::vector<long long> &k, int c0, int c1, int x, int y) {
     long long m = -1;
-    for (auto &b : nb) {
-      if (b[0] < 0 || b[0] >= h.txs || b[1] < 0 || b[1] >= h.tys) continue;
-      for (int c : {c0, c1})
-        if (c >= 0 && c < h.J) m = std::max(m, k[(size_t)c * h.nt + b[1] * h.txs + b[0]]);
+    for (int c : {c0, c1}) {
+      if (c < 0 || c >= h.J) continue;
+      const long long *kc = k.data() + (size_t)c * h.nt;
+      const int t = y * h.txs + x;
+      m = std::max(m, kc[t]);
+      if (x > 0) m = std::max(m, kc[t - 1]);
+      if (x + 1 < h.txs) m = std::max(m, kc[t + 1]);
+      if (y > 0) m = std::max(m, kc[t - h.txs]);
+      if (y + 1 < h.tys) m = std::max(m, kc[t + h.txs]);
     }
     return m;
   };
   std::vector<FlowItem> gen;
   std::vector<long long> key;
-  std::vector<int> shot_of;
   gen.reserve(total);
   key.reserve(total);
-  shot_of.reserve(total);
   for (int r = 0; r < nsteps; ++r) {
     for (size_t s = 0; s < shots.size(); ++s) {   // stress items of step r
       Shape &h = sh[s];
-      for (int j = 0; j < h.J; ++j)
-        for (int t = 0; t < h.nt; ++t) {
-          long long k = 2ll * ((long long)j * h.nt + t) + h.step_base;
-          if (r > 0) k = std::max(k, last_dep(h, h.kv_prev, j, j + 1, t) + gap);
-          h.ks[(size_t)j * h.nt + t] = k;
-          const int k0 = j * chunk, k1 = std::min((j + 1) * chunk, shots[s].nz);
-          gen.push_back(FlowItem{{shots[s].id, t, k0, k1}, 0, r, j, 0});
-          key.push_back(k);
-          shot_of.push_back((int)s);
-        }
+      for (int j = 0; j < h.J; ++j) {
+        const int k0 = j * chunk, k1 = std::min((j + 1) * chunk, shots[s].nz);
+        for (int y = 0, t = 0; y < h.tys; ++y)
+          for (int x = 0; x < h.txs; ++x, ++t) {
+            long long k = 2ll * ((long long)j * h.nt + t) + h.step_base;
+            if (r > 0) k = std::max(k, last_dep(h, h.kv_prev, j, j + 1, x, y) + gap);
+            h.ks[(size_t)j * h.nt + t] = k;
+            gen.push_back(FlowItem{{shots[s].id, t, k0, k1}, 0, r, j, 0});
+            key.push_back(k);
+          }
+      }
     }
     for (size_t s = 0; s < shots.size(); ++s) {   // velocity items of step r
       Shape &h = sh[s];
-      for (int j = 0; j < h.J; ++j)
-        for (int t = 0; t < h.nt; ++t) {
-          const long long k = last_dep(h, h.ks, j - 1, j, t) + gap;
-          h.kv[(size_t)j * h.nt + t] = k;
-          const int k0 = std::max(j * chunk - 1, 0), k1 = (j == h.J - 1) ? shots[s].nz : (j + 1) * chunk - 1;
-          gen.push_back(FlowItem{{shots[s].id, t, k0, k1}, 1, r, j, 0});
-          key.push_back(k);
-          shot_of.push_back((int)s);
-        }
+      for (int j = 0; j < h.J; ++j) {
+        const int k0 = std::max(j * chunk - 1, 0), k1 = (j == h.J - 1) ? shots[s].nz : (j + 1) * chunk - 1;
+        for (int y = 0, t = 0; y < h.tys; ++y)
+          for (int x = 0; x < h.txs; ++x, ++t) {
+            const long long k = last_dep(h, h.ks, j - 1, j, x, y) + gap;
+            h.kv[(size_t)j * h.nt + t] = k;
+            gen.push_back(FlowItem{{shots[s].id, t, k0, k1}, 1, r, j, 0});
+            key.push_back(k);
+          }
+      }
       h.kv_prev = h.kv;
       if (!overlap) h.step_base = *std::max_element(h.kv.begin(), h.kv.end()) + 1;
     }
@@ -288,37 +291,44 @@ bool build_flow_schedule(const std::vector<FlowShape> &shots, int tx, int ty, in
     for (size_t q = 0; q < n; ++q) order[q] = (unsigned)q;
     std::stable_sort(order.begin(), order.end(), [&](unsigned a, unsigned b) { return key[a] < key[b]; });
   }
-  // check: every item comes after every item it waits for
-  std::vector<std::vector<int>> pos(shots.size());
-  for (size_t s = 0; s < shots.size(); ++s) pos[s].assign((size_t)nsteps * 2 * sh[s].J * sh[s].nt, -1);
-  auto at = [&](int s, int r, int kind, int j, int t) -> int & {
-    return pos[s][(((size_t)r * 2 + kind) * sh[s].J + j) * sh[s].nt + t];
-  };
-  for (size_t q = 0; q < n; ++q) {
-    const FlowItem &f = gen[order[q]];
-    at(shot_of[order[q]], f.step, f.kind, f.chunk, f.it.tile) = (int)q;
-  }
-  for (size_t q = 0; q < n; ++q) {
-    const int s = shot_of[order[q]];
-    const FlowItem &f = gen[order[q]];
-    const Shape &h = sh[s];
-    const int tx0 = f.it.tile % h.txs, ty0 = f.it.tile / h.txs;
-    const int r = f.kind == 0 ? f.step - 1 : f.step;   // step of the items waited for
-    if (r < 0) continue;                               // before the launch: done
-    const int c0 = f.chunk, c1 = f.kind == 0 ? (f.chunk + 1 < h.J ? f.chunk + 1 : -1) : f.chunk - 1;
-    const int nb[5][2] = {{tx0, ty0}, {tx0 - 1, ty0}, {tx0 + 1, ty0}, {tx0, ty0 - 1}, {tx0, ty0 + 1}};
-    for (auto &b : nb) {
-      if (b[0] < 0 || b[0] >= h.txs || b[1] < 0 || b[1] >= h.tys) continue;
-      for (int c : {c0, c1}) {
-        if (c < 0) continue;
-        const int d = at(s, r, 1 - f.kind, c, b[1] * h.txs + b[0]);
-        if (d < 0 || d >= (int)q) {
-          *why = "dataflow schedule: an item does not follow the items it waits for";
-          return false;
+  // check: every item comes after every item it waits for.  Items are
+  // visited in generation order, where an item's index follows from (step,
+  // kind, shot, chunk, tile): step r, kind k, shot s start at
+  // r * 2 * per_kind + k * per_kind + first[s]
+  std::vector<unsigned> pos(n);
+  for (size_t q = 0; q < n; ++q) pos[order[q]] = (unsigned)q;
+  std::vector<size_t> first(shots.size() + 1, 0);
+  for (size_t s = 0; s < shots.size(); ++s) first[s + 1] = first[s] + (size_t)sh[s].J * sh[s].nt;
+  const size_t per_kind = first[shots.size()];
+  size_t g = 0;
+  for (int r = 0; r < nsteps; ++r)
+    for (int kind = 0; kind < 2; ++kind)
+      for (size_t s = 0; s < shots.size(); ++s) {
+        const Shape &h = sh[s];
+        const int rd = kind == 0 ? r - 1 : r;   // step of the items waited for
+        const size_t dep0 = rd < 0 ? 0 : ((size_t)rd * 2 + (1 - kind)) * per_kind + first[s];
+        for (int j = 0; j < h.J; ++j) {
+          const int c0 = j, c1 = kind == 0 ? j + 1 : j - 1;
+          for (int y = 0, t = 0; y < h.tys; ++y)
+            for (int x = 0; x < h.txs; ++x, ++t, ++g) {
+              if (rd < 0) continue;   // before the launch: done
+              const unsigned me = pos[g];
+              for (int c : {c0, c1}) {
+                if (c < 0 || c >= h.J) continue;
+                const size_t d = dep0 + (size_t)c * h.nt + t;
+                bool ok = pos[d] < me;
+                if (x > 0) ok = ok && pos[d - 1] < me;
+                if (x + 1 < h.txs) ok = ok && pos[d + 1] < me;
+                if (y > 0) ok = ok && pos[d - h.txs] < me;
+                if (y + 1 < h.tys) ok = ok && pos[d + h.txs] < me;
+                if (!ok) {
+                  *why = "dataflow schedule: an item does not follow the items it waits for";
+                  return false;
+                }
+              }
+            }
         }
       }
-    }
-  }
   items->resize(n);
   for (size_t q = 0; q < n; ++q) (*items)[q] = gen[order[q]];
   return true;
