@@ -238,21 +238,19 @@ bool build_flow_schedule(const std::vector<FlowShape> &shots, int tx, int ty, in
     }
     return m;
   };
-  std::vector<FlowItem> gen;
+  // keys in generation order (step, kind, shot, chunk, tile); the items
+  // themselves follow from that order and are written out once sorted
   std::vector<long long> key;
-  gen.reserve(total);
   key.reserve(total);
   for (int r = 0; r < nsteps; ++r) {
     for (size_t s = 0; s < shots.size(); ++s) {   // stress items of step r
       Shape &h = sh[s];
       for (int j = 0; j < h.J; ++j) {
-        const int k0 = j * chunk, k1 = std::min((j + 1) * chunk, shots[s].nz);
         for (int y = 0, t = 0; y < h.tys; ++y)
           for (int x = 0; x < h.txs; ++x, ++t) {
             long long k = 2ll * ((long long)j * h.nt + t) + h.step_base;
             if (r > 0) k = std::max(k, last_dep(h, h.kv_prev, j, j + 1, x, y) + gap);
             h.ks[(size_t)j * h.nt + t] = k;
-            gen.push_back(FlowItem{{shots[s].id, t, k0, k1}, 0, r, j, 0});
             key.push_back(k);
           }
       }
@@ -260,12 +258,10 @@ bool build_flow_schedule(const std::vector<FlowShape> &shots, int tx, int ty, in
     for (size_t s = 0; s < shots.size(); ++s) {   // velocity items of step r
       Shape &h = sh[s];
       for (int j = 0; j < h.J; ++j) {
-        const int k0 = std::max(j * chunk - 1, 0), k1 = (j == h.J - 1) ? shots[s].nz : (j + 1) * chunk - 1;
         for (int y = 0, t = 0; y < h.tys; ++y)
           for (int x = 0; x < h.txs; ++x, ++t) {
             const long long k = last_dep(h, h.ks, j - 1, j, x, y) + gap;
             h.kv[(size_t)j * h.nt + t] = k;
-            gen.push_back(FlowItem{{shots[s].id, t, k0, k1}, 1, r, j, 0});
             key.push_back(k);
           }
       }
@@ -274,7 +270,7 @@ bool build_flow_schedule(const std::vector<FlowShape> &shots, int tx, int ty, in
     }
   }
   // stable sort by key
-  const size_t n = gen.size();
+  const size_t n = key.size();
   std::vector<unsigned> order(n);
   long long kmin = 0, kmax = -1;
   if (n) {
@@ -330,7 +326,20 @@ bool build_flow_schedule(const std::vector<FlowShape> &shots, int tx, int ty, in
         }
       }
   items->resize(n);
-  for (size_t q = 0; q < n; ++q) (*items)[q] = gen[order[q]];
+  for (size_t q = 0; q < n; ++q) {   // the item of generation index order[q]
+    size_t g2 = order[q];
+    const int r = (int)(g2 / (2 * per_kind));
+    g2 -= (size_t)r * 2 * per_kind;
+    const int kind = g2 >= per_kind ? 1 : 0;
+    g2 -= (size_t)kind * per_kind;
+    const size_t sidx = (size_t)(std::upper_bound(first.begin(), first.end(), g2) - first.begin()) - 1;
+    g2 -= first[sidx];
+    const Shape &h = sh[sidx];
+    const int j = (int)(g2 / h.nt), t = (int)(g2 % h.nt), nz = shots[sidx].nz;
+    const int k0 = kind == 0 ? j * chunk : std::max(j * chunk - 1, 0);
+    const int k1 = kind == 0 ? std::min((j + 1) * chunk, nz) : (j == h.J - 1 ? nz : (j + 1) * chunk - 1);
+    (*items)[q] = FlowItem{{shots[sidx].id, t, k0, k1}, kind, r, j, 0};
+  }
   return true;
 }
 
