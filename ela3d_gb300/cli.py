@@ -33,6 +33,12 @@ from ._abi import Plan
 from .params import FP32, FP64, ShotParams
 
 
+# the keys of a parameter file (the C++ runner, ela3d_run.cpp, reads the same)
+KEYS = ("nx", "ny", "nz", "dx", "dt", "nstep", "sampgat", "it_output", "ngatx", "ngaty", "npml", "npower", "k_max",
+        "alpha_max", "rcoef", "vpml", "f0", "t0", "factor", "angle", "src", "src_kind", "stf", "w", "clean",
+        "energy_every", "model", "rec")
+
+
 def parse_params(path: str) -> tuple[ShotParams, dict]:
     kv = {}
     rec = []
@@ -41,6 +47,8 @@ def parse_params(path: str) -> tuple[ShotParams, dict]:
         if not parts or parts[0].startswith("#"):
             continue
         k, v = parts[0], parts[1:]
+        if k not in KEYS:
+            raise ValueError(f"{path}: unknown key {k!r} (known: {' '.join(KEYS)})")
         if k == "rec":
             rec.append([int(x) for x in v[:3]])
         else:
@@ -54,7 +62,8 @@ def parse_params(path: str) -> tuple[ShotParams, dict]:
                    factor=g("factor", 1e7), stf=g("stf", 0, int), src_kind=g("src_kind", 0, int),
                    src=tuple(int(x) for x in kv.get("src", ["16", "16", "16"])), sampgat=g("sampgat", 1, int),
                    src_w=tuple(float(x) for x in kv.get("w", ["0", "0", "1"])), angle_force=g("angle", 0.0),
-                   rec=np.array(rec, np.int32).reshape(-1, 3), it_output=g("it_output", 0, int))
+                   rec=np.array(rec, np.int32).reshape(-1, 3), it_output=g("it_output", 0, int),
+                   energy_every=g("energy_every", 0, int))
     extra = {"ngatx": g("ngatx", 0, int), "ngaty": g("ngaty", 0, int),
              "model": kv["model"][0] if "model" in kv else None}
     return p, extra

@@ -14,8 +14,9 @@
 // "w wx wy wz", clean (0/1 profile variant), energy_every, model PREFIX
 // (PREFIXcp.bin, PREFIXcs.bin, PREFIXrh.bin, float32 x fastest; without it
 // the reference's constant medium cp 3300, cs 3300/1.732, rho 3000), and
-// optional "rec i j k" lines.  Keys and defaults are those of the Python
-// runner (python -m ela3d_gb300 run), so both read the same file alike.
+// optional "rec i j k" lines; any other key is an error.  Keys and defaults
+// are those of the Python runner (python -m ela3d_gb300 run), so both read
+// the same file alike.
 //
 // Outputs, in the layouts of the reference's programs:
 //   rechorvx.txt rechorvy.txt rechorvz.txt  when ngatx and ngaty are given:
@@ -32,6 +33,7 @@
 // Exit status 0 on success, 1 on bad input, 2 when the library reports an
 // error (its message on stderr).
 #include <algorithm>
+#include <iterator>
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
@@ -76,6 +78,12 @@ bool parse(const std::string &path, Input *in) {
     if (!(ss >> k) || k[0] == '#') continue;
     std::vector<std::string> v;
     for (std::string t; ss >> t;) v.push_back(t);
+    static const char *const kKeys[] = {"nx", "ny", "nz", "dx", "dt", "nstep", "sampgat", "it_output", "ngatx",
+                                        "ngaty", "npml", "npower", "k_max", "alpha_max", "rcoef", "vpml", "f0",
+                                        "t0", "factor", "angle", "src", "src_kind", "stf", "w", "clean",
+                                        "energy_every", "model", "rec"};
+    if (std::none_of(std::begin(kKeys), std::end(kKeys), [&](const char *q) { return k == q; }))
+      return fail(path + ": unknown key " + k);
     if (k == "rec") {
       if (v.size() < 3) return fail("rec needs i j k");
       for (int q = 0; q < 3; ++q) rec.push_back(std::atoi(v[q].c_str()));
